@@ -1,0 +1,182 @@
+"""Python mirror of the cuPSS API over the C-ABI.
+
+``Evolver`` follows the reference's public C++ API (inc/cupss/evolver.h:14-86):
+same method names, argument meaning and return codes; parse errors raise
+``CupssError`` where the reference prints and exits.  ``Solver`` is the
+IR-level handle (fields, implicit/explicit q-monomials, noise) used by the
+batched and served forms and by tests.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+
+import numpy as np
+
+from . import capi
+
+
+class Solver:
+    """Owns one ``cupssgb_solver``: a system on an sx*sy*sz grid."""
+
+    def __init__(self, sx, sy=1, sz=1, dx=1.0, dy=1.0, dz=1.0, dt=0.01):
+        self.lib = capi.load()
+        h = C.c_void_p()
+        capi.check(self.lib.cupssgb_solver_create(sx, sy, sz, dx, dy, dz, dt, C.byref(h)))
+        self.h = h
+        self.shape = (sz, sy, sx)
+        self.N = sx * sy * sz
+
+    def close(self):
+        if self.h:
+            self.lib.cupssgb_solver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_field(self, dynamic: bool) -> int:
+        return capi.check(self.lib.cupssgb_solver_add_field(self.h, int(bool(dynamic))))
+
+    def set_implicit(self, f, pres):
+        arr, n = capi.pres_array(pres)
+        capi.check(self.lib.cupssgb_solver_set_implicit(self.h, f, arr, n))
+
+    def add_term(self, f, product, pres) -> int:
+        prod = (C.c_int * max(len(product), 1))(*product)
+        arr, n = capi.pres_array(pres)
+        return capi.check(self.lib.cupssgb_solver_add_term(self.h, f, prod, len(product), arr, n))
+
+    def set_term_pres(self, f, t, pres):
+        arr, n = capi.pres_array(pres)
+        capi.check(self.lib.cupssgb_solver_set_term_pres(self.h, f, t, arr, n))
+
+    def set_noise(self, f, amp):
+        if amp is None:
+            capi.check(self.lib.cupssgb_solver_set_noise(self.h, f, None))
+        else:
+            arr, _ = capi.pres_array([amp])
+            capi.check(self.lib.cupssgb_solver_set_noise(self.h, f, arr))
+
+    def set_seed(self, seed: int):
+        capi.check(self.lib.cupssgb_solver_set_seed(self.h, seed))
+
+    def prepare(self):
+        capi.check(self.lib.cupssgb_solver_prepare(self.h))
+
+    def set_real(self, f, arr):
+        a = np.ascontiguousarray(np.asarray(arr, np.float32).reshape(-1))
+        assert a.size == self.N
+        capi.check(self.lib.cupssgb_solver_set_real(self.h, f, capi.fptr(a)))
+
+    def advance(self, n=1):
+        capi.check(self.lib.cupssgb_solver_advance(self.h, n))
+
+    def synchronize(self):
+        capi.check(self.lib.cupssgb_solver_synchronize(self.h))
+
+    def get_real(self, f):
+        out = np.empty(self.N, np.float32)
+        capi.check(self.lib.cupssgb_solver_get_real(self.h, f, capi.fptr(out)))
+        return out.reshape(self.shape)
+
+    def get_fourier(self, f):
+        out = np.empty(2 * self.N, np.float32)
+        capi.check(self.lib.cupssgb_solver_get_fourier(self.h, f, capi.fptr(out)))
+        return (out[0::2] + 1j * out[1::2]).reshape(self.shape)
+
+    @property
+    def step_count(self):
+        return self.lib.cupssgb_solver_step_count(self.h)
+
+    @property
+    def launch_count(self):
+        return self.lib.cupssgb_solver_launch_count(self.h)
+
+    @property
+    def device_bytes(self):
+        return self.lib.cupssgb_solver_device_bytes(self.h)
+
+
+class Evolver:
+    """Mirror of the reference ``evolver`` (same method names as the C++ API)."""
+
+    def __init__(self, with_cuda, sx, sy=1, sz=1, dx=1.0, dy=1.0, dz=1.0, dt=0.01, write_every=1):
+        self.lib = capi.load()
+        h = C.c_void_p()
+        capi.check(self.lib.cupssgb_evolver_create(int(bool(with_cuda)), sx, sy, sz, dx, dy, dz, dt,
+                                                   write_every, C.byref(h)))
+        self.h = h
+        self.shape = (sz, sy, sx)
+        self.N = sx * sy * sz
+
+    def close(self):
+        if self.h:
+            self.lib.cupssgb_evolver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def createField(self, name, dynamic):
+        return capi.check(self.lib.cupssgb_evolver_create_field(self.h, name.encode(), int(bool(dynamic))))
+
+    def addParameter(self, name, value):
+        return capi.check(self.lib.cupssgb_evolver_add_parameter(self.h, name.encode(), float(value)))
+
+    def addEquation(self, eq):
+        return capi.check(self.lib.cupssgb_evolver_add_equation(self.h, eq.encode()))
+
+    def addNoise(self, name, amp):
+        return capi.check(self.lib.cupssgb_evolver_add_noise(self.h, name.encode(), amp.encode()))
+
+    def updateParameter(self, name, value):
+        return capi.check(self.lib.cupssgb_evolver_update_parameter(self.h, name.encode(), float(value)))
+
+    def getParameter(self, name):
+        return self.lib.cupssgb_evolver_get_parameter(self.h, name.encode())
+
+    def setOutputField(self, name, out):
+        return capi.check(self.lib.cupssgb_evolver_set_output_field(self.h, name.encode(), int(out)))
+
+    def setNoiseSeed(self, seed):
+        return capi.check(self.lib.cupssgb_evolver_set_seed(self.h, int(seed)))
+
+    def setReal(self, name, arr):
+        a = np.ascontiguousarray(np.asarray(arr, np.float32).reshape(-1))
+        assert a.size == self.N
+        return capi.check(self.lib.cupssgb_evolver_set_real(self.h, name.encode(), capi.fptr(a)))
+
+    def prepareProblem(self):
+        return capi.check(self.lib.cupssgb_evolver_prepare(self.h))
+
+    def advanceTime(self, n=1):
+        return capi.check(self.lib.cupssgb_evolver_advance(self.h, int(n)))
+
+    def writeOut(self):
+        return capi.check(self.lib.cupssgb_evolver_write_out(self.h))
+
+    def getReal(self, name):
+        out = np.empty(self.N, np.float32)
+        capi.check(self.lib.cupssgb_evolver_get_real(self.h, name.encode(), capi.fptr(out)))
+        return out.reshape(self.shape)
+
+    def getFourier(self, name):
+        out = np.empty(2 * self.N, np.float32)
+        capi.check(self.lib.cupssgb_evolver_get_fourier(self.h, name.encode(), capi.fptr(out)))
+        return (out[0::2] + 1j * out[1::2]).reshape(self.shape)
+
+    def getCurrentTimestep(self):
+        return self.lib.cupssgb_evolver_current_step(self.h)
+
+    def describe(self):
+        n = self.lib.cupssgb_evolver_describe(self.h, None, 0)
+        buf = C.create_string_buffer(n + 1)
+        self.lib.cupssgb_evolver_describe(self.h, buf, n + 1)
+        return json.loads(buf.value.decode())

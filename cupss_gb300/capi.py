@@ -1,0 +1,135 @@
+"""ctypes binding of the C-ABI declared in include/cupss_gb300.h.
+
+The shared library is the in-tree ``cupss_gb300/libcupss.so`` built by
+``cupss_gb300/build.py``.  Loading fails loudly if it is missing: there is no
+fallback implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcupss.so")
+
+OK = 0
+ERR_INVALID = -1
+ERR_CUDA = -2
+ERR_UNSUPPORTED = -3
+ERR_STATE = -4
+ERR_PARSE = -5
+ERR_LIMIT = -6
+
+
+class Pres(C.Structure):
+    """``cupssgb_pres`` == reference ``struct pres`` (inc/cupss/defines.h:31-39)."""
+    _fields_ = [("preFactor", C.c_float), ("q2n", C.c_int), ("iqx", C.c_int), ("iqy", C.c_int),
+                ("iqz", C.c_int), ("invq", C.c_int)]
+
+
+class CupssError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("cupss_gb300 error %d: %s" % (code, msg))
+        self.code = code
+
+
+_P = C.c_void_p
+_I = C.c_int
+_F = C.c_float
+_FP = C.POINTER(C.c_float)
+_IP = C.POINTER(C.c_int)
+_PP = C.POINTER(Pres)
+_S = C.c_char_p
+_LL = C.c_longlong
+_ULL = C.c_ulonglong
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "cupssgb_last_error": (_S, []),
+    "cupssgb_version": (_I, []),
+    "cupssgb_solver_create": (_I, [_I, _I, _I, _F, _F, _F, _F, C.POINTER(_P)]),
+    "cupssgb_solver_destroy": (_I, [_P]),
+    "cupssgb_solver_add_field": (_I, [_P, _I]),
+    "cupssgb_solver_set_implicit": (_I, [_P, _I, _PP, _I]),
+    "cupssgb_solver_update_implicit": (_I, [_P, _I, _PP, _I]),
+    "cupssgb_solver_add_term": (_I, [_P, _I, _IP, _I, _PP, _I]),
+    "cupssgb_solver_set_term_pres": (_I, [_P, _I, _I, _PP, _I]),
+    "cupssgb_solver_set_noise": (_I, [_P, _I, _PP]),
+    "cupssgb_solver_set_seed": (_I, [_P, _ULL]),
+    "cupssgb_solver_prepare": (_I, [_P]),
+    "cupssgb_solver_set_real": (_I, [_P, _I, _FP]),
+    "cupssgb_solver_set_real_device": (_I, [_P, _I, _P]),
+    "cupssgb_solver_advance": (_I, [_P, _I]),
+    "cupssgb_solver_get_real": (_I, [_P, _I, _FP]),
+    "cupssgb_solver_get_real_device": (_I, [_P, _I, _P]),
+    "cupssgb_solver_get_fourier": (_I, [_P, _I, _FP]),
+    "cupssgb_solver_get_fourier_device": (_I, [_P, _I, _P]),
+    "cupssgb_solver_synchronize": (_I, [_P]),
+    "cupssgb_solver_step_count": (_LL, [_P]),
+    "cupssgb_solver_launch_count": (_LL, [_P]),
+    "cupssgb_solver_device_bytes": (_LL, [_P]),
+    "cupssgb_solver_stream": (_P, [_P]),
+    "cupssgb_evolver_create": (_I, [_I, _I, _I, _I, _F, _F, _F, _F, _I, C.POINTER(_P)]),
+    "cupssgb_evolver_destroy": (_I, [_P]),
+    "cupssgb_evolver_create_field": (_I, [_P, _S, _I]),
+    "cupssgb_evolver_add_parameter": (_I, [_P, _S, _F]),
+    "cupssgb_evolver_add_equation": (_I, [_P, _S]),
+    "cupssgb_evolver_add_noise": (_I, [_P, _S, _S]),
+    "cupssgb_evolver_update_parameter": (_I, [_P, _S, _F]),
+    "cupssgb_evolver_set_output_field": (_I, [_P, _S, _I]),
+    "cupssgb_evolver_set_seed": (_I, [_P, _ULL]),
+    "cupssgb_evolver_set_real": (_I, [_P, _S, _FP]),
+    "cupssgb_evolver_prepare": (_I, [_P]),
+    "cupssgb_evolver_advance": (_I, [_P, _I]),
+    "cupssgb_evolver_write_out": (_I, [_P]),
+    "cupssgb_evolver_get_real": (_I, [_P, _S, _FP]),
+    "cupssgb_evolver_get_fourier": (_I, [_P, _S, _FP]),
+    "cupssgb_evolver_get_parameter": (_F, [_P, _S]),
+    "cupssgb_evolver_current_step": (_I, [_P]),
+    "cupssgb_evolver_describe": (_I, [_P, C.c_char_p, _I]),
+    "cupssgb_evolver_solver": (_P, [_P]),
+}
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Loads (once) and returns the C-ABI library with typed entry points."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise ImportError("cupss_gb300: %s is missing; run cupss_gb300/build.py (or "
+                          "__graft_entry__.build()) first -- there is no fallback" % p)
+    lib = C.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def check(code: int):
+    if code < 0:
+        raise CupssError(code, load().cupssgb_last_error().decode())
+    return code
+
+
+def fptr(arr):
+    import numpy as np
+    assert arr.dtype == np.float32 and arr.flags["C_CONTIGUOUS"]
+    return arr.ctypes.data_as(_FP)
+
+
+def pres_array(items):
+    n = len(items)
+    arr = (Pres * max(n, 1))()
+    for i, p in enumerate(items):
+        if isinstance(p, Pres):
+            arr[i] = p
+        else:
+            arr[i] = Pres(float(p[0]), *[int(v) for v in p[1:6]])
+    return arr, n

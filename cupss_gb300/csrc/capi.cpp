@@ -1,0 +1,439 @@
+// C-ABI entry points (declared in include/cupss_gb300.h).
+#include <cstdio>
+#include <cstring>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/cupss.h"
+#include "../../include/cupss_gb300.h"
+#include "engine.h"
+#include "host_common.h"
+
+struct cupssgb_solver {
+  cupssgb::Solver* s;
+};
+
+struct cupssgb_evolver {
+  evolver* e;
+};
+
+namespace {
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+template <class F>
+int guard(F&& fn) {
+  try {
+    g_last_error.clear();
+    return fn();
+  } catch (const cupssgb::Error& e) {
+    return fail(e.code, e.what());
+  } catch (const cupssgb_host::ParseError& e) {
+    return fail(CUPSSGB_ERR_PARSE, e.what());
+  } catch (const std::exception& e) {
+    return fail(CUPSSGB_ERR_INVALID, e.what());
+  } catch (...) {
+    return fail(CUPSSGB_ERR_INVALID, "unknown error");
+  }
+}
+
+std::vector<cupssgb::HostPres> to_host(const cupssgb_pres* p, int n) {
+  std::vector<cupssgb::HostPres> out;
+  for (int i = 0; i < n; ++i) {
+    cupssgb::HostPres h;
+    h.pre = p[i].preFactor;
+    h.q2n = p[i].q2n;
+    h.iqx = p[i].iqx;
+    h.iqy = p[i].iqy;
+    h.iqz = p[i].iqz;
+    h.invq = p[i].invq;
+    out.push_back(h);
+  }
+  return out;
+}
+
+#define NEED(ptr)                                                     \
+  if ((ptr) == nullptr) return fail(CUPSSGB_ERR_INVALID, #ptr " is NULL")
+
+void json_pres(std::ostringstream& os, const pres& p) {
+  char buf[160];
+  std::snprintf(buf, sizeof(buf), "[%.9g, %d, %d, %d, %d, %d]", (double)p.preFactor, p.q2n, p.iqx, p.iqy,
+                p.iqz, p.invq);
+  os << buf;
+}
+
+field* find_field(evolver* e, const char* name) {
+  if (!name) return nullptr;
+  auto it = e->fieldsMap.find(name);
+  return it == e->fieldsMap.end() ? nullptr : it->second;
+}
+}  // namespace
+
+extern "C" {
+
+const char* cupssgb_last_error(void) { return g_last_error.c_str(); }
+int cupssgb_version(void) { return 100; }
+
+// ---------------- solver level ----------------
+int cupssgb_solver_create(int sx, int sy, int sz, float dx, float dy, float dz, float dt,
+                          cupssgb_solver** out) {
+  NEED(out);
+  return guard([&] {
+    *out = new cupssgb_solver{new cupssgb::Solver(sx, sy, sz, dx, dy, dz, dt)};
+    return 0;
+  });
+}
+
+int cupssgb_solver_destroy(cupssgb_solver* s) {
+  if (!s) return 0;
+  return guard([&] {
+    delete s->s;
+    delete s;
+    return 0;
+  });
+}
+
+int cupssgb_solver_add_field(cupssgb_solver* s, int dynamic) {
+  NEED(s);
+  return guard([&] { return s->s->add_field(dynamic != 0); });
+}
+
+int cupssgb_solver_set_implicit(cupssgb_solver* s, int field, const cupssgb_pres* pres, int n) {
+  NEED(s);
+  if (n > 0 && !pres) return fail(CUPSSGB_ERR_INVALID, "pres is NULL");
+  return guard([&] {
+    s->s->set_implicit(field, to_host(pres, n));
+    return 0;
+  });
+}
+
+int cupssgb_solver_update_implicit(cupssgb_solver* s, int field, const cupssgb_pres* pres, int n) {
+  return cupssgb_solver_set_implicit(s, field, pres, n);
+}
+
+int cupssgb_solver_add_term(cupssgb_solver* s, int field, const int* product, int n_product,
+                            const cupssgb_pres* pres, int n_pres) {
+  NEED(s);
+  if ((n_product > 0 && !product) || !pres || n_pres <= 0 || n_product < 0)
+    return fail(CUPSSGB_ERR_INVALID, "bad term arguments");
+  return guard([&] {
+    return s->s->add_term(field, std::vector<int>(product, product + n_product), to_host(pres, n_pres));
+  });
+}
+
+int cupssgb_solver_set_term_pres(cupssgb_solver* s, int field, int term, const cupssgb_pres* pres, int n) {
+  NEED(s);
+  NEED(pres);
+  return guard([&] {
+    s->s->set_term_pres(field, term, to_host(pres, n));
+    return 0;
+  });
+}
+
+int cupssgb_solver_set_noise(cupssgb_solver* s, int field, const cupssgb_pres* amp) {
+  NEED(s);
+  return guard([&] {
+    cupssgb::HostPres h;
+    if (amp) h = to_host(amp, 1)[0];
+    s->s->set_noise(field, amp != nullptr, h);
+    return 0;
+  });
+}
+
+int cupssgb_solver_set_seed(cupssgb_solver* s, unsigned long long seed) {
+  NEED(s);
+  s->s->set_seed(seed);
+  return 0;
+}
+
+int cupssgb_solver_prepare(cupssgb_solver* s) {
+  NEED(s);
+  return guard([&] {
+    s->s->prepare();
+    return 0;
+  });
+}
+
+int cupssgb_solver_set_real(cupssgb_solver* s, int field, const float* host_real) {
+  NEED(s);
+  NEED(host_real);
+  return guard([&] {
+    s->s->set_real(field, host_real, false);
+    s->s->synchronize();
+    return 0;
+  });
+}
+
+int cupssgb_solver_set_real_device(cupssgb_solver* s, int field, const float* dev_real) {
+  NEED(s);
+  NEED(dev_real);
+  return guard([&] {
+    s->s->set_real(field, dev_real, true);
+    return 0;
+  });
+}
+
+int cupssgb_solver_advance(cupssgb_solver* s, int nsteps) {
+  NEED(s);
+  if (nsteps < 0) return fail(CUPSSGB_ERR_INVALID, "nsteps < 0");
+  return guard([&] {
+    s->s->advance(nsteps);
+    return 0;
+  });
+}
+
+int cupssgb_solver_get_real(cupssgb_solver* s, int field, float* host_real) {
+  NEED(s);
+  NEED(host_real);
+  return guard([&] {
+    s->s->get_real(field, host_real, false);
+    return 0;
+  });
+}
+
+int cupssgb_solver_get_real_device(cupssgb_solver* s, int field, float* dev_real) {
+  NEED(s);
+  NEED(dev_real);
+  return guard([&] {
+    s->s->get_real(field, dev_real, true);
+    return 0;
+  });
+}
+
+int cupssgb_solver_get_fourier(cupssgb_solver* s, int field, float* host_complex) {
+  NEED(s);
+  NEED(host_complex);
+  return guard([&] {
+    s->s->get_fourier(field, reinterpret_cast<float2*>(host_complex), false);
+    return 0;
+  });
+}
+
+int cupssgb_solver_get_fourier_device(cupssgb_solver* s, int field, float* dev_complex) {
+  NEED(s);
+  NEED(dev_complex);
+  return guard([&] {
+    s->s->get_fourier(field, reinterpret_cast<float2*>(dev_complex), true);
+    return 0;
+  });
+}
+
+int cupssgb_solver_synchronize(cupssgb_solver* s) {
+  NEED(s);
+  return guard([&] {
+    s->s->synchronize();
+    return 0;
+  });
+}
+
+long long cupssgb_solver_step_count(const cupssgb_solver* s) { return s ? s->s->step_count() : -1; }
+long long cupssgb_solver_launch_count(const cupssgb_solver* s) { return s ? s->s->launches() : -1; }
+long long cupssgb_solver_device_bytes(const cupssgb_solver* s) {
+  return s ? (long long)s->s->device_bytes() : -1;
+}
+void* cupssgb_solver_stream(const cupssgb_solver* s) { return s ? (void*)s->s->stream() : nullptr; }
+
+// ---------------- evolver level ----------------
+int cupssgb_evolver_create(int with_cuda, int sx, int sy, int sz, float dx, float dy, float dz, float dt,
+                           int write_every, cupssgb_evolver** out) {
+  NEED(out);
+  if (sx < 1 || sy < 1 || sz < 1 || write_every < 1) return fail(CUPSSGB_ERR_INVALID, "bad sizes");
+  return guard([&] {
+    evolver* e;
+    if (sy == 1 && sz == 1) e = new evolver(with_cuda != 0, sx, dx, dt, write_every);
+    else if (sz == 1) e = new evolver(with_cuda != 0, sx, sy, dx, dy, dt, write_every);
+    else e = new evolver(with_cuda != 0, sx, sy, sz, dx, dy, dz, dt, write_every);
+    e->setThrowOnError(true);
+    *out = new cupssgb_evolver{e};
+    return 0;
+  });
+}
+
+int cupssgb_evolver_destroy(cupssgb_evolver* e) {
+  if (!e) return 0;
+  return guard([&] {
+    delete e->e;
+    delete e;
+    return 0;
+  });
+}
+
+int cupssgb_evolver_create_field(cupssgb_evolver* e, const char* name, int dynamic) {
+  NEED(e);
+  NEED(name);
+  return guard([&] {
+    int r = e->e->createField(name, dynamic != 0);
+    return r == 0 ? 0 : fail(CUPSSGB_ERR_INVALID, std::string("field exists: ") + name);
+  });
+}
+
+int cupssgb_evolver_add_parameter(cupssgb_evolver* e, const char* name, float value) {
+  NEED(e);
+  NEED(name);
+  return guard([&] {
+    int r = e->e->_parser->insert_parameter(name, value);
+    return r == 0 ? 0 : fail(CUPSSGB_ERR_INVALID, std::string("duplicate parameter ") + name);
+  });
+}
+
+int cupssgb_evolver_add_equation(cupssgb_evolver* e, const char* equation) {
+  NEED(e);
+  NEED(equation);
+  return guard([&] { return e->e->addEquation(equation); });
+}
+
+int cupssgb_evolver_add_noise(cupssgb_evolver* e, const char* field_name, const char* amplitude) {
+  NEED(e);
+  NEED(field_name);
+  NEED(amplitude);
+  return guard([&] {
+    int r = e->e->addNoise(field_name, amplitude);
+    return r == 0 ? 0 : fail(CUPSSGB_ERR_INVALID, std::string("no field ") + field_name);
+  });
+}
+
+int cupssgb_evolver_update_parameter(cupssgb_evolver* e, const char* name, float value) {
+  NEED(e);
+  NEED(name);
+  return guard([&] { return e->e->updateParameter(name, value); });
+}
+
+int cupssgb_evolver_set_output_field(cupssgb_evolver* e, const char* name, int output) {
+  NEED(e);
+  NEED(name);
+  return guard([&] {
+    if (!find_field(e->e, name)) return fail(CUPSSGB_ERR_INVALID, std::string("no field ") + name);
+    e->e->setOutputField(name, output);
+    return 0;
+  });
+}
+
+int cupssgb_evolver_set_seed(cupssgb_evolver* e, unsigned long long seed) {
+  NEED(e);
+  e->e->setNoiseSeed(seed);
+  return 0;
+}
+
+int cupssgb_evolver_set_real(cupssgb_evolver* e, const char* name, const float* host_real) {
+  NEED(e);
+  NEED(host_real);
+  return guard([&] {
+    field* f = find_field(e->e, name);
+    if (!f) return fail(CUPSSGB_ERR_INVALID, std::string("no field ") + (name ? name : ""));
+    const size_t n = (size_t)e->e->getSystemSizeX() * e->e->getSystemSizeY() * e->e->getSystemSizeZ();
+    for (size_t i = 0; i < n; ++i) f->real_array[i].x = host_real[i];
+    return 0;
+  });
+}
+
+int cupssgb_evolver_prepare(cupssgb_evolver* e) {
+  NEED(e);
+  return guard([&] {
+    e->e->prepareProblem();
+    return 0;
+  });
+}
+
+int cupssgb_evolver_advance(cupssgb_evolver* e, int nsteps) {
+  NEED(e);
+  if (nsteps < 0) return fail(CUPSSGB_ERR_INVALID, "nsteps < 0");
+  return guard([&] { return e->e->advanceTimeSteps(nsteps); });
+}
+
+int cupssgb_evolver_write_out(cupssgb_evolver* e) {
+  NEED(e);
+  return guard([&] {
+    e->e->writeOut();
+    return 0;
+  });
+}
+
+int cupssgb_evolver_get_real(cupssgb_evolver* e, const char* name, float* host_real) {
+  NEED(e);
+  NEED(host_real);
+  return guard([&] {
+    const int idx = e->e->existsField(name ? name : "");
+    if (idx < 0) return fail(CUPSSGB_ERR_INVALID, std::string("no field ") + (name ? name : ""));
+    cupssgb_solver* s = e->e->solverHandle();
+    if (!s) return fail(CUPSSGB_ERR_STATE, "prepareProblem has not been called");
+    return cupssgb_solver_get_real(s, idx, host_real);
+  });
+}
+
+int cupssgb_evolver_get_fourier(cupssgb_evolver* e, const char* name, float* host_complex) {
+  NEED(e);
+  NEED(host_complex);
+  return guard([&] {
+    const int idx = e->e->existsField(name ? name : "");
+    if (idx < 0) return fail(CUPSSGB_ERR_INVALID, std::string("no field ") + (name ? name : ""));
+    cupssgb_solver* s = e->e->solverHandle();
+    if (!s) return fail(CUPSSGB_ERR_STATE, "prepareProblem has not been called");
+    return cupssgb_solver_get_fourier(s, idx, host_complex);
+  });
+}
+
+float cupssgb_evolver_get_parameter(cupssgb_evolver* e, const char* name) {
+  if (!e || !name) return 0.f;
+  float v = 0.f;
+  guard([&] {
+    v = e->e->getParameter(name);
+    return 0;
+  });
+  return v;
+}
+
+int cupssgb_evolver_current_step(const cupssgb_evolver* e) {
+  return e ? const_cast<evolver*>(e->e)->getCurrentTimestep() : -1;
+}
+
+int cupssgb_evolver_describe(const cupssgb_evolver* ce, char* buf, int buflen) {
+  NEED(ce);
+  evolver* e = ce->e;
+  std::ostringstream os;
+  os << "[";
+  for (size_t i = 0; i < e->fields.size(); ++i) {
+    field* f = e->fields[i];
+    if (i) os << ", ";
+    os << "{\"name\": \"" << f->name << "\", \"dynamic\": " << (f->dynamic ? "true" : "false")
+       << ", \"implicit\": [";
+    for (size_t j = 0; j < f->implicit.size(); ++j) {
+      if (j) os << ", ";
+      json_pres(os, f->implicit[j]);
+    }
+    os << "], \"terms\": [";
+    for (size_t t = 0; t < f->terms.size(); ++t) {
+      if (t) os << ", ";
+      os << "{\"product\": [";
+      for (size_t k = 0; k < f->terms[t]->product.size(); ++k) {
+        if (k) os << ", ";
+        os << "\"" << f->terms[t]->product[k]->name << "\"";
+      }
+      os << "], \"pres\": [";
+      for (size_t k = 0; k < f->terms[t]->prefactors_h.size(); ++k) {
+        if (k) os << ", ";
+        json_pres(os, f->terms[t]->prefactors_h[k]);
+      }
+      os << "]}";
+    }
+    os << "], \"noisy\": " << (f->isNoisy ? "true" : "false") << ", \"noise\": ";
+    json_pres(os, f->noise_amplitude);
+    os << "}";
+  }
+  os << "]";
+  const std::string s = os.str();
+  if (buf && buflen > 0) {
+    const size_t n = std::min((size_t)buflen - 1, s.size());
+    std::memcpy(buf, s.data(), n);
+    buf[n] = 0;
+  }
+  return (int)s.size();
+}
+
+cupssgb_solver* cupssgb_evolver_solver(cupssgb_evolver* e) { return e ? e->e->solverHandle() : nullptr; }
+
+}  // extern "C"

@@ -1,0 +1,490 @@
+// GB300 pseudospectral engine: plan compilation, device buffers, step driver.
+#include "engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <sstream>
+
+#include "launch.h"
+
+namespace cupssgb {
+
+namespace {
+constexpr float kPiF = 3.1415926535f;   // the reference's PI (inc/cupss/defines.h:57)
+
+bool pow2(int n) { return n >= 1 && (n & (n - 1)) == 0; }
+
+std::string cuda_msg(cudaError_t e, const char* what) {
+  std::ostringstream os;
+  os << what << ": " << cudaGetErrorString(e);
+  return os.str();
+}
+}  // namespace
+
+Solver::Solver(int sx, int sy, int sz, float dx, float dy, float dz, float dt)
+    : sx_(sx), sy_(sy), sz_(sz), dx_(dx), dy_(dy), dz_(dz), dt_(dt) {
+  if (!pow2(sx) || sx < 2 || sx > 2048 || !pow2(sy) || sy > 1024 || !pow2(sz) || sz > 1024)
+    throw Error(kErrUnsupported,
+                "grid sizes must be powers of two: 2 <= sx <= 2048, 1 <= sy, sz <= 1024");
+  // dimension rule of the reference (src/evolver.cpp:22-36)
+  dim_ = (sz == 1 && sy == 1) ? 1 : (sz == 1 ? 2 : 3);
+  Lx_ = sx / 2;
+  // field constructor q-steps (src/field_init.cpp:207-213), float arithmetic
+  stepq_[0] = 2.0f * kPiF / (dx * (float)sx);
+  stepq_[1] = 2.0f * kPiF / (dy * (float)sy);
+  stepq_[2] = 2.0f * kPiF / (dz * (float)sz);
+}
+
+Solver::~Solver() {
+  if (stream_) cudaStreamSynchronize(stream_);
+  for (void* p : allocs_) cudaFree(p);
+  if (stream_) cudaStreamDestroy(stream_);
+}
+
+void Solver::check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw Error(kErrCuda, cuda_msg(e, what));
+}
+
+void* Solver::dalloc(size_t bytes) {
+  void* p = nullptr;
+  check(cudaMalloc(&p, bytes), "cudaMalloc");
+  allocs_.push_back(p);
+  dev_bytes_ += bytes;
+  check(cudaMemsetAsync(p, 0, bytes, stream_), "cudaMemsetAsync");
+  return p;
+}
+
+int Solver::add_field(bool dynamic) {
+  if (prepared_) throw Error(kErrState, "add_field after prepare");
+  if ((int)fields_.size() >= kMaxFields) throw Error(kErrLimit, "too many fields");
+  HostField f;
+  f.dynamic = dynamic;
+  fields_.push_back(f);
+  return (int)fields_.size() - 1;
+}
+
+void Solver::set_implicit(int f, const std::vector<HostPres>& p) {
+  if (f < 0 || f >= nfields()) throw Error(kErrInvalid, "bad field index");
+  if (prepared_ && p.size() != fields_[f].implicit.size())
+    throw Error(kErrState, "the number of implicit prefactors cannot change after prepare");
+  fields_[f].implicit = p;
+}
+
+int Solver::add_term(int f, const std::vector<int>& product, const std::vector<HostPres>& p) {
+  if (f < 0 || f >= nfields()) throw Error(kErrInvalid, "bad field index");
+  if (prepared_) throw Error(kErrState, "add_term after prepare");
+  if (p.empty()) throw Error(kErrInvalid, "term without prefactors");
+  for (int g : product)
+    if (g < 0 || g >= nfields()) throw Error(kErrInvalid, "bad product field index");
+  if ((int)product.size() > kMaxOrder) throw Error(kErrLimit, "product order too large");
+  HostTerm t;
+  t.product = product;
+  t.pres = p;
+  fields_[f].terms.push_back(t);
+  return (int)fields_[f].terms.size() - 1;
+}
+
+void Solver::set_term_pres(int f, int t, const std::vector<HostPres>& p) {
+  if (f < 0 || f >= nfields() || t < 0 || t >= (int)fields_[f].terms.size())
+    throw Error(kErrInvalid, "bad term index");
+  if (p.size() != fields_[f].terms[t].pres.size())
+    throw Error(kErrInvalid, "prefactor count of a term cannot change");
+  fields_[f].terms[t].pres = p;
+}
+
+void Solver::set_noise(int f, bool on, const HostPres& amp) {
+  if (f < 0 || f >= nfields()) throw Error(kErrInvalid, "bad field index");
+  fields_[f].noisy = on;
+  fields_[f].noise = amp;
+}
+
+void Solver::set_dt(float dt) { dt_ = dt; }
+
+void Solver::build_plan() {
+  const int F = nfields();
+  alias_order_.assign(F, 1);
+  // term::prepareDevice (src/term_init.cpp:108-133): fields in products of size >= 2
+  // are dealiased for the largest such product.
+  for (const HostField& f : fields_)
+    for (const HostTerm& t : f.terms)
+      if (t.product.size() >= 2)
+        for (int g : t.product)
+          alias_order_[g] = std::max(alias_order_[g], (int)t.product.size());
+  for (int ph = 0; ph < 2; ++ph) {
+    Phase& P = phases_[ph];
+    P = Phase();
+    for (int f = 0; f < F; ++f)
+      if ((int)fields_[f].dynamic == ph) P.fields.push_back(f);
+    for (int f : P.fields) {
+      for (const HostTerm& t : fields_[f].terms) {
+        if (t.product.size() < 2) {
+          P.term_slot.push_back(-1);
+          continue;
+        }
+        std::vector<int> key = t.product;
+        std::sort(key.begin(), key.end());
+        auto it = std::find(P.products.begin(), P.products.end(), key);
+        int slot;
+        if (it == P.products.end()) {
+          P.products.push_back(key);
+          slot = (int)P.products.size() - 1;
+        } else {
+          slot = (int)(it - P.products.begin());
+        }
+        P.term_slot.push_back(slot);
+        for (int g : key)
+          if (std::find(P.xin.begin(), P.xin.end(), g) == P.xin.end()) P.xin.push_back(g);
+      }
+    }
+    if ((int)P.fields.size() > kMaxPhaseFields) throw Error(kErrLimit, "too many fields in a phase");
+    if ((int)P.products.size() > kMaxProd) throw Error(kErrLimit, "too many distinct products");
+    if ((int)P.xin.size() > kMaxXIn) throw Error(kErrLimit, "too many fields in products");
+    int nt = 0, np = 0;
+    for (int f : P.fields) {
+      nt += (int)fields_[f].terms.size();
+      np += (int)fields_[f].implicit.size();
+      for (const HostTerm& t : fields_[f].terms) np += (int)t.pres.size();
+    }
+    if (nt > kMaxTerms) throw Error(kErrLimit, "too many terms in a phase");
+    if (np > kMaxPres) throw Error(kErrLimit, "too many prefactors in a phase");
+  }
+}
+
+void Solver::prepare() {
+  if (prepared_) throw Error(kErrState, "prepare called twice");
+  int dev = 0;
+  check(cudaGetDevice(&dev), "cudaGetDevice");
+  check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+  build_plan();
+  const size_t half = (size_t)Lx_ * sy_ * sz_;
+  const int F = nfields();
+  // twiddle super-table: table for length L at offset L, L = 1..2048
+  {
+    const int Lmax = 2048;
+    std::vector<float2> h(2 * Lmax);
+    h[0] = make_float2(0.f, 0.f);
+    for (int L = 1; L <= Lmax; L *= 2)
+      for (int j = 0; j < L; ++j) {
+        const double a = -2.0 * M_PI * (double)j / (double)L;
+        h[L + j] = make_float2((float)std::cos(a), (float)std::sin(a));
+      }
+    tw_ = (float2*)dalloc(h.size() * sizeof(float2));
+    check(cudaMemcpyAsync(tw_, h.data(), h.size() * sizeof(float2), cudaMemcpyHostToDevice, stream_),
+          "twiddle upload");
+  }
+  state_[0].assign(F, nullptr);
+  state_[1].assign(F, nullptr);
+  chan_.assign(F, nullptr);
+  chanz_.assign(F, nullptr);
+  par_.assign(F, 0);
+  for (int f = 0; f < F; ++f) {
+    state_[0][f] = (float2*)dalloc(half * sizeof(float2));
+    state_[1][f] = (float2*)dalloc(half * sizeof(float2));
+    if (alias_order_[f] > 1) {
+      chan_[f] = (float2*)dalloc(half * sizeof(float2));
+      if (dim_ == 3) chanz_[f] = (float2*)dalloc(half * sizeof(float2));
+    }
+  }
+  for (Phase& P : phases_)
+    for (size_t j = 0; j < P.products.size(); ++j)
+      P.prodbuf.push_back((float2*)dalloc(half * sizeof(float2)));
+  scratch_real_ = (float*)dalloc(npoints() * sizeof(float));
+  scratch_spec_ = (float2*)dalloc(half * sizeof(float2));
+  check(cudaStreamSynchronize(stream_), "prepare sync");
+  prepared_ = true;
+}
+
+int Solver::pick_w(int L, int nl, int nslots) const {
+  int W = 16;
+  while (W > Lx_) W /= 2;
+  if (W < 1) W = 1;
+  while (W > 1 && (line_threads(L, nl, W) > 512 ||
+                   line_pass_smem(L, nl, W, std::max(nslots, 1)) > 200 * 1024))
+    W /= 2;
+  if (line_pass_smem(L, nl, W, std::max(nslots, 1)) > 220 * 1024)
+    throw Error(kErrLimit, "phase needs more shared memory than one CTA has");
+  return W;
+}
+
+void Solver::fill_line_common(LineParams& p, int L, int geo, int mode) const {
+  std::memset(&p, 0, sizeof(p));
+  p.sx = sx_;
+  p.sy = sy_;
+  p.sz = sz_;
+  p.Lx = Lx_;
+  p.L = L;
+  p.geo = geo;
+  p.mode = mode;
+  p.stepqx = stepq_[0];
+  p.stepqy = stepq_[1];
+  p.stepqz = stepq_[2];
+  p.dt = dt_;
+  const double N = (double)npoints();
+  p.invN = 1.0f / (float)N;   // normalize_k (src/field_kernels.cu:124)
+  p.sqrtN = (float)std::sqrt(N);
+  p.sqrtHalfN = (float)std::sqrt(N / 2.0);
+  p.tw = tw_;
+}
+
+void Solver::line_fwd_inv(int geo, int mode, const float2* in, float2* out, int xlimit) {
+  LineParams p;
+  const int L = (geo == kGeoY3 || geo == kGeoCol) ? sy_ : sz_;
+  fill_line_common(p, L, geo, mode);
+  p.W = pick_w(L, 1, 1);
+  p.n_prod = 1;
+  p.prod_in[0] = in;
+  p.prod_out[0] = out;
+  p.inv_xlimit[0] = xlimit;
+  dim3 grid((Lx_ + p.W - 1) / p.W, geo == kGeoY3 ? sz_ : (geo == kGeoZ3 ? sy_ : 1));
+  check(launch_line_pass(p, 1, 1, grid, stream_), "line pass");
+  ++launches_;
+}
+
+void Solver::set_real(int f, const float* src, bool on_device) {
+  if (!prepared_) throw Error(kErrState, "set_real before prepare");
+  if (f < 0 || f >= nfields()) throw Error(kErrInvalid, "bad field index");
+  const size_t n = npoints();
+  check(cudaMemcpyAsync(scratch_real_, src, n * sizeof(float),
+                        on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream_),
+        "set_real copy");
+  float2* st = state_[par_[f]][f];
+  XParams x;
+  std::memset(&x, 0, sizeof(x));
+  x.Lx = Lx_;
+  x.rows = sy_ * sz_;
+  x.in_mode = kXInReal;
+  x.out_mode = kXOutSpectral;
+  x.out_scale = 1.f;
+  x.n_in = 1;
+  x.in[0] = reinterpret_cast<const float2*>(scratch_real_);
+  x.n_prod = 1;
+  x.out[0] = st;
+  x.prod_n[0] = 1;
+  x.prod_f[0][0] = 0;
+  x.tw = tw_;
+  check(launch_row_pass(x, stream_), "row pass (upload)");
+  ++launches_;
+  if (dim_ == 3) {
+    line_fwd_inv(kGeoY3, kModeFwd, st, st, Lx_);
+    line_fwd_inv(kGeoZ3, kModeFwd, st, st, Lx_);
+  } else if (sy_ > 1) {
+    line_fwd_inv(kGeoCol, kModeFwd, st, st, Lx_);
+  }
+}
+
+void Solver::to_real_scratch(int f) {
+  const float2* st = state_[par_[f]][f];
+  const float2* spec = st;
+  if (dim_ == 3) {
+    line_fwd_inv(kGeoZ3, kModeInv, st, scratch_spec_, Lx_);
+    line_fwd_inv(kGeoY3, kModeInv, scratch_spec_, scratch_spec_, Lx_);
+    spec = scratch_spec_;
+  } else if (sy_ > 1) {
+    line_fwd_inv(kGeoCol, kModeInv, st, scratch_spec_, Lx_);
+    spec = scratch_spec_;
+  }
+  XParams x;
+  std::memset(&x, 0, sizeof(x));
+  x.Lx = Lx_;
+  x.rows = sy_ * sz_;
+  x.in_mode = kXInSpectral;
+  x.out_mode = kXOutReal;
+  x.out_scale = 1.0f / (float)npoints();
+  x.n_in = 1;
+  x.in[0] = spec;
+  x.n_prod = 1;
+  x.out[0] = scratch_real_;
+  x.prod_n[0] = 1;
+  x.prod_f[0][0] = 0;
+  x.tw = tw_;
+  check(launch_row_pass(x, stream_), "row pass (materialise)");
+  ++launches_;
+}
+
+void Solver::get_real(int f, float* dst, bool on_device) {
+  if (!prepared_) throw Error(kErrState, "get_real before prepare");
+  if (f < 0 || f >= nfields()) throw Error(kErrInvalid, "bad field index");
+  to_real_scratch(f);
+  check(cudaMemcpyAsync(dst, scratch_real_, npoints() * sizeof(float),
+                        on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, stream_),
+        "get_real copy");
+  if (!on_device) check(cudaStreamSynchronize(stream_), "get_real sync");
+}
+
+void Solver::get_real_pairs_device(int f, float2* dst) {
+  if (!prepared_) throw Error(kErrState, "get_real before prepare");
+  to_real_scratch(f);
+  // widen into the reference's float2 (x, 0) layout with a copy2D: x <- real, y <- 0
+  check(cudaMemsetAsync(dst, 0, npoints() * sizeof(float2), stream_), "memset pairs");
+  check(cudaMemcpy2DAsync(dst, sizeof(float2), scratch_real_, sizeof(float), sizeof(float), npoints(),
+                          cudaMemcpyDeviceToDevice, stream_),
+        "widen pairs");
+}
+
+void Solver::get_fourier(int f, float2* dst, bool on_device) {
+  if (!prepared_) throw Error(kErrState, "get_fourier before prepare");
+  if (f < 0 || f >= nfields()) throw Error(kErrInvalid, "bad field index");
+  float2* out = dst;
+  if (!on_device) {
+    if (!scratch_full_) scratch_full_ = (float2*)dalloc(npoints() * sizeof(float2));
+    out = scratch_full_;
+  }
+  ExpandParams e;
+  e.sx = sx_;
+  e.sy = sy_;
+  e.sz = sz_;
+  e.Lx = Lx_;
+  e.spec = state_[par_[f]][f];
+  e.full = out;
+  check(launch_expand(e, stream_), "expand spectrum");
+  ++launches_;
+  if (!on_device) {
+    check(cudaMemcpyAsync(dst, scratch_full_, npoints() * sizeof(float2), cudaMemcpyDeviceToHost,
+                          stream_),
+          "get_fourier copy");
+    check(cudaStreamSynchronize(stream_), "get_fourier sync");
+  }
+}
+
+void Solver::synchronize() {
+  if (stream_) check(cudaStreamSynchronize(stream_), "synchronize");
+}
+
+void Solver::run_phase(Phase& P) {
+  if (P.fields.empty()) return;
+  // ---- row pass: real-space products of the dealiased copies ----
+  if (!P.products.empty()) {
+    XParams x;
+    std::memset(&x, 0, sizeof(x));
+    x.Lx = Lx_;
+    x.rows = sy_ * sz_;
+    x.in_mode = kXInSpectral;
+    x.out_mode = kXOutSpectral;
+    x.out_scale = 1.f;
+    x.n_in = (int)P.xin.size();
+    for (int i = 0; i < x.n_in; ++i) x.in[i] = chan_[P.xin[i]];
+    x.n_prod = (int)P.products.size();
+    for (int q = 0; q < x.n_prod; ++q) {
+      x.out[q] = P.prodbuf[q];
+      x.prod_n[q] = (int)P.products[q].size();
+      for (int t = 0; t < x.prod_n[q]; ++t) {
+        const int g = P.products[q][t];
+        x.prod_f[q][t] = (int)(std::find(P.xin.begin(), P.xin.end(), g) - P.xin.begin());
+      }
+    }
+    x.tw = tw_;
+    check(launch_row_pass(x, stream_), "row pass");
+    ++launches_;
+    if (dim_ == 3) {
+      for (size_t q = 0; q < P.products.size(); ++q)
+        line_fwd_inv(kGeoY3, kModeFwd, P.prodbuf[q], P.prodbuf[q], Lx_);
+    }
+  }
+  // ---- turnaround ----
+  const int geo = (dim_ == 3) ? kGeoZ3 : kGeoCol;
+  const int L = (dim_ == 3) ? sz_ : sy_;
+  const int nl = (dim_ == 3) ? 2 : 1;
+  LineParams p;
+  fill_line_common(p, L, geo, kModeTurn);
+  p.n_prod = (int)P.products.size();
+  for (int q = 0; q < p.n_prod; ++q) p.prod_in[q] = P.prodbuf[q];
+  for (int g = 0; g < nfields(); ++g) p.state[g] = state_[par_[g]][g];
+  p.key0 = (uint32_t)(seed_ & 0xffffffffu);
+  p.key1 = (uint32_t)(seed_ >> 32);
+  p.step = (uint32_t)step_;
+  p.nf = (int)P.fields.size();
+  int nt = 0, npres = 0, ts = 0;
+  bool any_chan = false;
+  for (int fi = 0; fi < p.nf; ++fi) {
+    const int f = P.fields[fi];
+    const HostField& hf = fields_[f];
+    FieldK& K = p.f[fi];
+    K.cur = state_[par_[f]][f];
+    K.next = state_[par_[f] ^ 1][f];
+    K.chan = (alias_order_[f] > 1) ? (dim_ == 3 ? chanz_[f] : chan_[f]) : nullptr;
+    any_chan = any_chan || (K.chan != nullptr);
+    K.dynamic = hf.dynamic ? 1 : 0;
+    K.noisy = hf.noisy ? 1 : 0;
+    K.order = alias_order_[f];
+    K.fid = f;
+    K.chan_xlimit = sx_ / (K.order + 1);
+    K.chan_ylimit = sy_ / (K.order + 1);
+    K.term0 = nt;
+    K.nterms = (int)hf.terms.size();
+    for (size_t t = 0; t < hf.terms.size(); ++t, ++ts) {
+      const HostTerm& ht = hf.terms[t];
+      TermK& T = p.term[nt++];
+      if (ht.product.empty()) {
+        T.kind = kTermConst;
+        T.src = 0;
+      } else if (ht.product.size() == 1) {
+        T.kind = kTermSingle;
+        T.src = ht.product[0];
+      } else {
+        T.kind = kTermProduct;
+        T.src = P.term_slot[ts];
+      }
+      // precomputePrefactors sign rule (src/term_init.cpp:145-156)
+      const int s = (ht.pres[0].iqx + ht.pres[0].iqy + ht.pres[0].iqz) % 2;
+      T.s = s;
+      T.pres0 = npres;
+      T.npres = (int)ht.pres.size();
+      for (const HostPres& hp : ht.pres) {
+        const int u = hp.iqx + hp.iqy + hp.iqz;
+        const int negate = -2 * (((u - s) / 2) % 2) + 1;
+        PresK& K2 = p.pres[npres++];
+        K2.pre = hp.pre * (float)negate;
+        K2.q2n = hp.q2n;
+        K2.iqx = hp.iqx;
+        K2.iqy = hp.iqy;
+        K2.iqz = hp.iqz;
+        K2.invq = hp.invq;
+      }
+    }
+    K.imp0 = npres;
+    K.nimp = (int)hf.implicit.size();
+    for (const HostPres& hp : hf.implicit) {
+      PresK& K2 = p.pres[npres++];
+      K2.pre = hp.pre;
+      K2.q2n = hp.q2n;
+      K2.iqx = hp.iqx;
+      K2.iqy = hp.iqy;
+      K2.iqz = hp.iqz;
+      K2.invq = hp.invq;
+    }
+    if (hf.noisy) {
+      // precalculateImplicit noise factor (src/field_init.cpp:239-241, 269-278)
+      const float ddx = (float)(2.0 * (double)kPiF / (double)(stepq_[0] * (float)sx_));
+      const float ddy = (float)(2.0 * (double)kPiF / (double)(stepq_[1] * (float)sy_));
+      const float ddz = (float)(2.0 * (double)kPiF / (double)(stepq_[2] * (float)sz_));
+      float base = std::sqrt(dt_ / (ddx * ddy * ddz) * hf.noise.pre);
+      if (!hf.dynamic) base *= 1.0f / std::sqrt(dt_);   // setNotDynamic_k (field_kernels.cu:155)
+      K.noise_base = base;
+      K.noise_q2n = hf.noise.q2n;
+      K.noise_invq = hf.noise.invq;
+    }
+  }
+  const int nslots = p.n_prod + (any_chan ? 1 : 0);
+  p.W = pick_w(L, nl, nslots);
+  dim3 grid((Lx_ + p.W - 1) / p.W, dim_ == 3 ? std::max(sy_ / 2, 1) : 1);
+  check(launch_line_pass(p, nl, nslots, grid, stream_), "turnaround");
+  ++launches_;
+  for (int f : P.fields) par_[f] ^= 1;
+  if (dim_ == 3 && any_chan) {
+    for (int f : P.fields)
+      if (alias_order_[f] > 1) line_fwd_inv(kGeoY3, kModeInv, chanz_[f], chan_[f], sx_ / (alias_order_[f] + 1));
+  }
+}
+
+void Solver::advance(int nsteps) {
+  if (!prepared_) throw Error(kErrState, "advance before prepare");
+  for (int s = 0; s < nsteps; ++s) {
+    run_phase(phases_[0]);
+    run_phase(phases_[1]);
+    ++step_;
+  }
+}
+
+}  // namespace cupssgb

@@ -1,0 +1,134 @@
+// GB300 pseudospectral engine: host planner and device state for one system.
+//
+// A system is a set of scalar fields on an sx*sy*sz periodic grid.  Each field
+// carries implicit q-monomials, explicit terms (a product of fields times a sum of
+// q-monomials) and optional Gaussian noise -- exactly the IR that the reference's
+// parser produces (src/parser.cpp:628-767) and that its field/term classes execute
+// (src/field.cpp, src/term.cpp).  The engine executes one reference time step
+// (src/evolver.cpp:199-226) as two phases (non-dynamic fields, then dynamic ones),
+// each phase = [row pass computing the real-space products] + [line-pass turnaround
+// doing the Fourier-space update], with 3D adding a y-axis pass on either side.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+#include "engine_types.h"
+
+namespace cupssgb {
+
+enum Status : int {
+  kOk = 0,
+  kErrInvalid = -1,
+  kErrCuda = -2,
+  kErrUnsupported = -3,
+  kErrState = -4,
+  kErrParse = -5,
+  kErrLimit = -6,
+};
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& msg) : std::runtime_error(msg), code(c) {}
+};
+
+struct HostPres {
+  float pre = 0.f;
+  int q2n = 0, iqx = 0, iqy = 0, iqz = 0, invq = 0;
+};
+
+struct HostTerm {
+  std::vector<int> product;     // field indices, any order (multiset)
+  std::vector<HostPres> pres;
+};
+
+struct HostField {
+  bool dynamic = false;
+  std::vector<HostPres> implicit;
+  std::vector<HostTerm> terms;
+  bool noisy = false;
+  HostPres noise;
+};
+
+class Solver {
+ public:
+  Solver(int sx, int sy, int sz, float dx, float dy, float dz, float dt);
+  ~Solver();
+  Solver(const Solver&) = delete;
+  Solver& operator=(const Solver&) = delete;
+
+  int add_field(bool dynamic);
+  void set_implicit(int f, const std::vector<HostPres>& p);
+  int add_term(int f, const std::vector<int>& product, const std::vector<HostPres>& p);
+  void set_term_pres(int f, int t, const std::vector<HostPres>& p);
+  void set_noise(int f, bool on, const HostPres& amp);
+  void set_seed(uint64_t s) { seed_ = s; }
+  void set_dt(float dt);
+
+  void prepare();
+  bool prepared() const { return prepared_; }
+  void set_real(int f, const float* src, bool src_on_device);
+  void advance(int nsteps);
+  void get_real(int f, float* dst, bool dst_on_device);
+  void get_fourier(int f, float2* dst, bool dst_on_device);
+  void get_real_pairs_device(int f, float2* dst);   // reference float2 layout (x, 0)
+  void synchronize();
+
+  int sx() const { return sx_; }
+  int sy() const { return sy_; }
+  int sz() const { return sz_; }
+  int dim() const { return dim_; }
+  size_t npoints() const { return (size_t)sx_ * sy_ * sz_; }
+  int nfields() const { return (int)fields_.size(); }
+  long long step_count() const { return step_; }
+  long long launches() const { return launches_; }
+  cudaStream_t stream() const { return stream_; }
+  size_t device_bytes() const { return dev_bytes_; }
+  const HostField& field(int f) const { return fields_.at(f); }
+  bool needs_alias(int f) const { return alias_order_.at(f) > 1; }
+  int alias_order(int f) const { return alias_order_.at(f); }
+
+ private:
+  struct Phase {
+    std::vector<int> fields;                 // fields updated in this phase
+    std::vector<std::vector<int>> products;  // sorted multisets (size >= 2)
+    std::vector<int> xin;                    // fields feeding the row pass
+    std::vector<float2*> prodbuf;
+    std::vector<int> term_slot;              // per (field, term) flattened: product slot or -1
+  };
+
+  void check(cudaError_t e, const char* what);
+  void* dalloc(size_t bytes);
+  void build_plan();
+  void run_phase(Phase& ph);
+  void fill_line_common(LineParams& p, int L, int geo, int mode) const;
+  int pick_w(int L, int nl, int nslots) const;
+  void line_fwd_inv(int geo, int mode, const float2* in, float2* out, int xlimit);
+  void to_real_scratch(int f);
+
+  int sx_, sy_, sz_, dim_, Lx_;
+  float dx_, dy_, dz_, dt_;
+  float stepq_[3];
+  uint64_t seed_ = 0x243F6A8885A308D3ull;
+  std::vector<HostField> fields_;
+  std::vector<int> alias_order_;
+  bool prepared_ = false;
+  long long step_ = 0;
+  long long launches_ = 0;
+  size_t dev_bytes_ = 0;
+
+  cudaStream_t stream_ = nullptr;
+  float2* tw_ = nullptr;
+  std::vector<float2*> state_[2];
+  std::vector<int> par_;
+  std::vector<float2*> chan_;    // row-pass input (x spectrum, y/z positional)
+  std::vector<float2*> chanz_;   // 3D: z-inverse output before the y-inverse
+  float* scratch_real_ = nullptr;
+  float2* scratch_spec_ = nullptr;
+  float2* scratch_full_ = nullptr;   // reference-layout full spectrum, allocated on first use
+  std::vector<void*> allocs_;
+  Phase phases_[2];              // 0: non-dynamic, 1: dynamic
+};
+
+}  // namespace cupssgb

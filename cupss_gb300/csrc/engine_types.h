@@ -1,0 +1,105 @@
+// Parameter blocks shared by the host planner and the CUDA kernels.
+//
+// Spectral storage ("packed half spectrum"): a real field of sx*sy*sz points is
+// held as Lx*sy*sz complex values, Lx = sx/2, index ((kz*sy + ky)*Lx + kx').
+// Column kx' = 0 packs the two real-in-x planes kx = 0 and kx = sx/2:
+//   Z(ky,kz) = F(0,ky,kz) + i F(sx/2,ky,kz),
+// so F(0,k) = (Z(k) + conj Z(-k))/2 and F(sx/2,k) = -i (Z(k) - conj Z(-k))/2.
+// Columns 0 < kx' < sx/2 hold F(kx',ky,kz); kx > sx/2 follow by Hermitian symmetry.
+// This is the same information as the reference's full C2C float2 array after its
+// per-step projection onto real fields (src/field.cpp:63-89), in half the bytes.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace cupssgb {
+
+constexpr int kMaxXIn = 8;         // real-space inputs of one row pass
+constexpr int kMaxProd = 8;        // products per phase
+constexpr int kMaxOrder = 8;       // factors per product
+constexpr int kMaxPhaseFields = 12;
+constexpr int kMaxTerms = 24;
+constexpr int kMaxPres = 48;
+constexpr int kMaxFields = 32;
+
+// One q-monomial: pre * q^(2 q2n) * qx^iqx * qy^iqy * qz^iqz * |q|^-invq.
+// For explicit terms `pre` already carries the reference's sign rule
+// (src/term_init.cpp:151-152); the factor i is applied per term via TermK::s.
+struct PresK {
+  float pre;
+  int q2n, iqx, iqy, iqz, invq;
+};
+
+enum TermKind : int { kTermSingle = 0, kTermProduct = 1, kTermConst = 2 };
+
+struct TermK {
+  int kind;    // TermKind
+  int src;     // field index (single) or product slot (product)
+  int s;       // 1 -> multiply by i (odd number of iq factors in the first pres)
+  int npres, pres0;
+};
+
+struct FieldK {
+  const float2* cur;     // state at the start of the phase
+  float2* next;          // state after the phase (ping-pong partner)
+  float2* chan;          // masked, 1/N-scaled inverse along the line axis, or null
+  int dynamic, noisy;
+  int nterms, term0;
+  int nimp, imp0;
+  int order;             // dealias order (max product size the field appears in)
+  int fid;               // field id used in the noise counter
+  float noise_base;      // sqrt(dt/dV*A) (dynamic) or that / sqrt(dt) (non-dynamic)
+  int noise_q2n, noise_invq;
+  int chan_xlimit;       // last kx' column with unmasked content (sx/(order+1))
+  int chan_ylimit;       // |n_y| limit (sy/(order+1)), used to skip empty 3D tiles
+};
+
+enum LineGeo : int {
+  kGeoCol = 0,   // 1D/2D: lines are y-columns, elem = y*Lx + kx'
+  kGeoY3 = 1,    // 3D y lines, elem = (z*sy + y)*Lx + kx', blockIdx.y = z
+  kGeoZ3 = 2,    // 3D z lines, elem = (z*sy + ky)*Lx + kx', blockIdx.y = ky (or pair)
+};
+
+enum LineMode : int { kModeTurn = 0, kModeFwd = 1, kModeInv = 2 };
+
+struct LineParams {
+  int sx, sy, sz, Lx, L;
+  int geo, mode, W;
+  float stepqx, stepqy, stepqz, dt, invN, sqrtN, sqrtHalfN;
+  // products (turnaround) or channels to transform (fwd/inv passes)
+  int n_prod;
+  const float2* prod_in[kMaxProd];
+  float2* prod_out[kMaxProd];       // fwd/inv passes only (may equal prod_in)
+  int inv_xlimit[kMaxProd];         // inv pass: skip tiles with kx0 > limit
+  int nf;
+  FieldK f[kMaxPhaseFields];
+  TermK term[kMaxTerms];
+  PresK pres[kMaxPres];             // term pres, then implicit pres (raw, unsigned)
+  const float2* state[kMaxFields];  // current state of every field
+  uint32_t key0, key1, step;
+  const float2* tw;
+};
+
+enum XInMode : int { kXInSpectral = 0, kXInReal = 1 };
+enum XOutMode : int { kXOutSpectral = 0, kXOutReal = 1, kXOutRealPair = 2 };
+
+struct XParams {
+  int Lx, rows;
+  int in_mode, out_mode;
+  float out_scale;
+  int n_in;
+  const float2* in[kMaxXIn];        // spectral channels (float2) or real rows (as pairs)
+  int n_prod;
+  void* out[kMaxProd];
+  int prod_n[kMaxProd];
+  int prod_f[kMaxProd][kMaxOrder];
+  const float2* tw;
+};
+
+struct ExpandParams {
+  int sx, sy, sz, Lx;
+  const float2* spec;   // packed half spectrum, fully transformed
+  float2* full;         // reference layout, sx*sy*sz complex
+};
+
+}  // namespace cupssgb

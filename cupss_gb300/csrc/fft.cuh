@@ -1,0 +1,193 @@
+// Register/shared-memory FFT building blocks for the GB300 pseudospectral engine.
+//
+// A line of length L (power of two, 1..1024) is split as L = R * M with
+// M = 2^floor(log2(L)/2) and R = L / M (so R is M or 2M).  M threads cooperate on
+// one line; each thread holds R complex values in registers.
+//
+//   step-1 layout: thread m holds positions  n = m + M*r,            r in [0,R)
+//   step-2 layout: thread m holds positions  k = s + R*k',  s = m + M*j,
+//                  j in [0, R/M), k' in [0,M)   (register index j*M + k')
+//
+// Forward transform (unnormalised, exp(-2 pi i n k / L)):
+//   fwd_step1 (radix-R DFT over r, twiddle W_L^{m s}), store to the transpose
+//   buffer at position s*M + m, sync, load positions s*M + k, fwd_step2 (radix-M).
+// Inverse transform (unnormalised, exp(+2 pi i n k / L)) runs the same steps
+// backwards: inv_step2 in step-2 layout, transpose, inv_step1.
+//
+// The four-step split X[s + R k'] = sum_m W_M^{m k'} W_L^{m s} sum_r x[m + M r] W_R^{r s}
+// is the standard Cooley-Tukey factorisation; the register DFTs are recursive
+// radix-2 decimation in time with compile-time twiddles.
+#pragma once
+#include <cuda_runtime.h>
+#include <utility>
+#include "twiddle32.h"
+
+#if defined(__CUDACC__)
+#define CG_HD __host__ __device__ __forceinline__
+#else
+#define CG_HD inline
+#endif
+
+namespace cupssgb {
+
+CG_HD float2 c_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+CG_HD float2 c_sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+CG_HD float2 c_mul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * conj(b)
+CG_HD float2 c_mulc(float2 a, float2 b) {
+  return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+CG_HD float2 c_conj(float2 a) { return make_float2(a.x, -a.y); }
+CG_HD float2 c_scale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+CG_HD float2 c_muli(float2 a) { return make_float2(-a.y, a.x); }    // i * a
+CG_HD float2 c_mulmi(float2 a) { return make_float2(a.y, -a.x); }   // -i * a
+
+// Multiply by W_N^K (forward, W = exp(-2 pi i/N)) or its conjugate (INV), N <= 32.
+template <int N, int K, bool INV>
+CG_HD float2 tw_const(float2 a) {
+  constexpr int k = K % N;
+  if constexpr (k == 0) {
+    return a;
+  } else if constexpr (4 * k == N) {
+    return INV ? c_muli(a) : c_mulmi(a);
+  } else if constexpr (2 * k == N) {
+    return make_float2(-a.x, -a.y);
+  } else if constexpr (4 * k == 3 * N) {
+    return INV ? c_mulmi(a) : c_muli(a);
+  } else {
+    constexpr int j = k * (32 / N);
+    constexpr float wr = kTw32Re[j];
+    constexpr float wi = INV ? -kTw32Im[j] : kTw32Im[j];
+    return c_mul(a, make_float2(wr, wi));
+  }
+}
+
+// In-place DFT of the N values v[O + S*i], i in [0,N), natural-order output.
+template <int N, bool INV, int S>
+struct Dft {
+  template <int O, int K0, int... K>
+  CG_HD static void combine(float2* v, std::integer_sequence<int, K0, K...>) {
+    constexpr int H = N / 2;
+    float2 ev[H];
+#pragma unroll
+    for (int q = 0; q < H; ++q) ev[q] = v[O + 2 * S * q];
+    float2 od[H] = {tw_const<N, K0, INV>(v[O + S + 2 * S * K0]),
+                    tw_const<N, K, INV>(v[O + S + 2 * S * K])...};
+#pragma unroll
+    for (int q = 0; q < H; ++q) {
+      v[O + S * q] = c_add(ev[q], od[q]);
+      v[O + S * (q + H)] = c_sub(ev[q], od[q]);
+    }
+  }
+  template <int O>
+  CG_HD static void run(float2* v) {
+    if constexpr (N == 1) {
+      return;
+    } else if constexpr (N == 2) {
+      float2 a = v[O], b = v[O + S];
+      v[O] = c_add(a, b);
+      v[O + S] = c_sub(a, b);
+    } else {
+      Dft<N / 2, INV, 2 * S>::template run<O>(v);
+      Dft<N / 2, INV, 2 * S>::template run<O + S>(v);
+      combine<O>(v, std::make_integer_sequence<int, N / 2>{});
+    }
+  }
+};
+
+template <int L>
+struct LineCfg {
+  static constexpr int lg = (L <= 1) ? 0 : (L == 2 ? 1 : (L == 4 ? 2 : (L == 8 ? 3 : (L == 16 ? 4 :
+                            (L == 32 ? 5 : (L == 64 ? 6 : (L == 128 ? 7 : (L == 256 ? 8 :
+                            (L == 512 ? 9 : (L == 1024 ? 10 : -1))))))))));
+  static_assert(lg >= 0, "line length must be a power of two in [1, 1024]");
+  static constexpr int M = 1 << (lg / 2);
+  static constexpr int R = L / M;
+  static constexpr int J = R / M;   // s-values per thread in step 2 (1 or 2)
+};
+
+// Twiddle super-table: the table for length L lives at tw + L and holds
+// exp(-2 pi i j / L) for j in [0, L).
+CG_HD float2 tw_load(const float2* tw, int L, int j) {
+#if defined(__CUDA_ARCH__)
+  return __ldg(tw + L + j);
+#else
+  return tw[L + j];
+#endif
+}
+
+template <int L, bool INV>
+CG_HD void step_r(float2 (&v)[LineCfg<L>::R]) {
+  Dft<LineCfg<L>::R, INV, 1>::template run<0>(v);
+}
+
+// Forward step 1: v[r] = x[m + M r] in, v[s] = W_L^{m s} * DFT_R(x[m + M .])[s] out.
+template <int L>
+CG_HD void fwd_step1(float2 (&v)[LineCfg<L>::R], int m, const float2* tw) {
+  constexpr int R = LineCfg<L>::R;
+  Dft<R, false, 1>::template run<0>(v);
+#pragma unroll
+  for (int s = 1; s < R; ++s) v[s] = c_mul(v[s], tw_load(tw, L, m * s));
+}
+
+// Forward step 2: register index j*M + k holds position s*M + k (s = m + M j) of the
+// transposed data; output register j*M + k' holds X[s + R k'].
+template <int L>
+CG_HD void fwd_step2(float2 (&v)[LineCfg<L>::R]) {
+  constexpr int M = LineCfg<L>::M;
+  constexpr int J = LineCfg<L>::J;
+  if constexpr (J >= 1) Dft<M, false, 1>::template run<0>(v);
+  if constexpr (J >= 2) Dft<M, false, 1>::template run<M>(v);
+}
+
+// Inverse step 2: register j*M + k' holds X[s + R k']; out register j*M + m' holds
+// y_{m'}[s] = sum_k' X[s + R k'] W_M^{-m' k'}  (to be stored at position s*M + m').
+template <int L>
+CG_HD void inv_step2(float2 (&v)[LineCfg<L>::R]) {
+  constexpr int M = LineCfg<L>::M;
+  constexpr int J = LineCfg<L>::J;
+  if constexpr (J >= 1) Dft<M, true, 1>::template run<0>(v);
+  if constexpr (J >= 2) Dft<M, true, 1>::template run<M>(v);
+}
+
+// Inverse step 1: v[s] = y_m[s] (loaded from positions s*M + m) in,
+// v[r] = x[m + M r] out.
+template <int L>
+CG_HD void inv_step1(float2 (&v)[LineCfg<L>::R], int m, const float2* tw) {
+  constexpr int R = LineCfg<L>::R;
+#pragma unroll
+  for (int s = 1; s < R; ++s) v[s] = c_mulc(v[s], tw_load(tw, L, m * s));
+  Dft<R, true, 1>::template run<0>(v);
+}
+
+// Position of register index idx in the step-1 / step-2 layouts.
+template <int L>
+CG_HD int pos_step1(int m, int r) { return m + LineCfg<L>::M * r; }
+template <int L>
+CG_HD int pos_step2(int m, int idx) {
+  constexpr int M = LineCfg<L>::M;
+  constexpr int R = LineCfg<L>::R;
+  const int j = idx / M, kp = idx % M;
+  return (m + M * j) + R * kp;
+}
+// Transpose-buffer position written after fwd_step1 for value s, and read before
+// fwd_step2 for register index idx (= j*M + k).
+template <int L>
+CG_HD int pos_t1(int m, int s) { return s * LineCfg<L>::M + m; }
+template <int L>
+CG_HD int pos_t2(int m, int idx) {
+  constexpr int M = LineCfg<L>::M;
+  const int j = idx / M, k = idx % M;
+  return (m + M * j) * M + k;
+}
+
+// Padded shared-memory index of position n: one pad slot every M positions keeps
+// the strided step-2 accesses free of bank conflicts.
+template <int L>
+CG_HD int pad_pos(int n) { return n + n / LineCfg<L>::M; }
+template <int L>
+CG_HD constexpr int padded_len() { return L + L / LineCfg<L>::M; }
+
+}  // namespace cupssgb

@@ -1,0 +1,29 @@
+"""Writes twiddle32.h: exp(-2*pi*i*j/32), j in [0,32), as exact float hex literals.
+
+The register-level DFTs (radix <= 32) take their internal twiddles from this
+table at compile time.  Values are computed in double and rounded once to float.
+"""
+import math
+import os
+import struct
+
+
+def f32hex(v):
+    if abs(v) < 1e-12:          # exact zeros at multiples of pi/2
+        v = 0.0
+    f = struct.unpack("f", struct.pack("f", v))[0]
+    return float(f).hex() + "f" if f != 0.0 else "0.0f"
+
+
+lines = ["// Generated by gen_twiddle32.py -- do not edit.",
+         "#pragma once",
+         "namespace cupssgb {",
+         "// kTw32Re[j] + i*kTw32Im[j] = exp(-2*pi*i*j/32)",
+         "__host__ __device__ constexpr float kTw32Re[32] = {"]
+lines.append(", ".join(f32hex(math.cos(2 * math.pi * j / 32)) for j in range(32)) + "};")
+lines.append("__host__ __device__ constexpr float kTw32Im[32] = {")
+lines.append(", ".join(f32hex(-math.sin(2 * math.pi * j / 32)) for j in range(32)) + "};")
+lines.append("}  // namespace cupssgb")
+here = os.path.dirname(os.path.abspath(__file__))
+with open(os.path.join(here, "twiddle32.h"), "w") as fh:
+    fh.write("\n".join(lines) + "\n")

@@ -1,0 +1,2 @@
+#include "k_line_inst.cuh"
+CUPSSGB_LINE_INST(1024)

@@ -1,0 +1,68 @@
+// Line-pass dispatch and the spectrum expansion kernel.
+#include "kernels.cuh"
+#include "launch.h"
+
+namespace cupssgb {
+
+static int m_of(int L) {
+  int lg = 0;
+  while ((1 << lg) < L) ++lg;
+  return 1 << (lg / 2);
+}
+static int pl_of(int L) { return L + L / m_of(L); }
+
+size_t line_pass_smem(int L, int nl, int W, int nslots) {
+  return (size_t)nslots * nl * pl_of(L) * W * sizeof(float2);
+}
+int line_threads(int L, int nl, int W) { return W * m_of(L) * nl; }
+
+cudaError_t launch_line_pass(const LineParams& p, int nl, int nslots, dim3 grid, cudaStream_t st) {
+  const size_t smem = line_pass_smem(p.L, nl, p.W, nslots > 0 ? nslots : 1);
+  switch (p.L) {
+    case 1: return launch_line_1(p, nl, smem, grid, st);
+    case 2: return launch_line_2(p, nl, smem, grid, st);
+    case 4: return launch_line_4(p, nl, smem, grid, st);
+    case 8: return launch_line_8(p, nl, smem, grid, st);
+    case 16: return launch_line_16(p, nl, smem, grid, st);
+    case 32: return launch_line_32(p, nl, smem, grid, st);
+    case 64: return launch_line_64(p, nl, smem, grid, st);
+    case 128: return launch_line_128(p, nl, smem, grid, st);
+    case 256: return launch_line_256(p, nl, smem, grid, st);
+    case 512: return launch_line_512(p, nl, smem, grid, st);
+    case 1024: return launch_line_1024(p, nl, smem, grid, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+__global__ void expand_spectrum(const ExpandParams p) {
+  const size_t N = (size_t)p.sx * p.sy * p.sz;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < N;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int kx = (int)(idx % p.sx);
+    const int ky = (int)((idx / p.sx) % p.sy);
+    const int kz = (int)(idx / ((size_t)p.sx * p.sy));
+    const int pky = (p.sy - ky) & (p.sy - 1);
+    const int pkz = (p.sz - kz) & (p.sz - 1);
+    float2 out;
+    if (kx > 0 && 2 * kx < p.sx) {
+      out = p.spec[((size_t)kz * p.sy + ky) * p.Lx + kx];
+    } else if (2 * kx > p.sx) {
+      out = c_conj(p.spec[((size_t)pkz * p.sy + pky) * p.Lx + (p.sx - kx)]);
+    } else {
+      const float2 z = p.spec[((size_t)kz * p.sy + ky) * p.Lx];
+      const float2 zp = p.spec[((size_t)pkz * p.sy + pky) * p.Lx];
+      out = unpack(z, zp, kx == 0 ? 0 : 1);
+    }
+    p.full[idx] = out;
+  }
+}
+
+cudaError_t launch_expand(const ExpandParams& p, cudaStream_t st) {
+  const size_t N = (size_t)p.sx * p.sy * p.sz;
+  int blocks = (int)((N + 255) / 256);
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  expand_spectrum<<<blocks, 256, 0, st>>>(p);
+  return cudaGetLastError();
+}
+
+}  // namespace cupssgb

@@ -1,0 +1,28 @@
+// Host-side launchers for the engine kernels (implemented in k_*.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include "engine_types.h"
+
+namespace cupssgb {
+
+// Row pass over all rows; picks the template by p.Lx.
+cudaError_t launch_row_pass(const XParams& p, cudaStream_t st);
+size_t row_pass_smem(int Lx, int n_in);
+
+// Line pass: grid.x = ceil(Lx/W) tiles, grid.y per geometry; nl = 2 for the paired
+// 3D z-turnaround.  nslots = shared-memory slots the mode needs.
+cudaError_t launch_line_pass(const LineParams& p, int nl, int nslots, dim3 grid, cudaStream_t st);
+size_t line_pass_smem(int L, int nl, int W, int nslots);
+int line_threads(int L, int nl, int W);
+
+cudaError_t launch_expand(const ExpandParams& p, cudaStream_t st);
+
+// per-L launchers (one translation unit per group of sizes)
+#define CUPSSGB_DECL_LINE(L) \
+  cudaError_t launch_line_##L(const LineParams& p, int nl, size_t smem, dim3 grid, cudaStream_t st);
+CUPSSGB_DECL_LINE(1) CUPSSGB_DECL_LINE(2) CUPSSGB_DECL_LINE(4) CUPSSGB_DECL_LINE(8)
+CUPSSGB_DECL_LINE(16) CUPSSGB_DECL_LINE(32) CUPSSGB_DECL_LINE(64) CUPSSGB_DECL_LINE(128)
+CUPSSGB_DECL_LINE(256) CUPSSGB_DECL_LINE(512) CUPSSGB_DECL_LINE(1024)
+#undef CUPSSGB_DECL_LINE
+
+}  // namespace cupssgb

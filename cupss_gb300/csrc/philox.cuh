@@ -1,0 +1,47 @@
+// Counter-based Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers:
+// as easy as 1, 2, 3", SC'11) and a Box-Muller normal pair.
+//
+// Replaces the reference's host-API cuRAND Philox generator + real-space noise FFT
+// (src/field_init.cpp:130-137, src/field.cpp:300-316): the noise is drawn directly in
+// Fourier space inside the update, so it costs no memory traffic.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace cupssgb {
+
+#if defined(__CUDACC__)
+__device__ __forceinline__ void philox4x32_10(uint32_t& c0, uint32_t& c1, uint32_t& c2, uint32_t& c3,
+                                              uint32_t k0, uint32_t k1) {
+  constexpr uint32_t kM0 = 0xD2511F53u, kM1 = 0xCD9E8D57u;
+  constexpr uint32_t kW0 = 0x9E3779B9u, kW1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t hi0 = __umulhi(kM0, c0), lo0 = kM0 * c0;
+    const uint32_t hi1 = __umulhi(kM1, c2), lo1 = kM1 * c2;
+    const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0;
+    c1 = lo1;
+    c2 = n2;
+    c3 = lo0;
+    k0 += kW0;
+    k1 += kW1;
+  }
+}
+
+// Two standard normals from counter (ctr, step, fid, 0) under key (k0, k1).
+__device__ __forceinline__ void philox_normal2(uint32_t ctr, uint32_t step, uint32_t fid,
+                                               uint32_t k0, uint32_t k1, float& g1, float& g2) {
+  uint32_t c0 = ctr, c1 = step, c2 = fid, c3 = 0u;
+  philox4x32_10(c0, c1, c2, c3, k0, k1);
+  const float u1 = (float)((c0 >> 8) + 1u) * 5.9604644775390625e-08f;   // (0, 1]
+  const float u2 = (float)(c1 >> 8) * 5.9604644775390625e-08f;          // [0, 1)
+  const float r = sqrtf(-2.0f * logf(u1));
+  float s, c;
+  sincospif(2.0f * u2, &s, &c);
+  g1 = r * c;
+  g2 = r * s;
+}
+#endif
+
+}  // namespace cupssgb

@@ -1,0 +1,159 @@
+/* C-ABI of the GB300-native cuPSS pseudospectral step.
+ *
+ * Two levels, both plain C (no C++ or torch types in the signatures):
+ *
+ *  1. Solver level (cupssgb_solver_*): a system given directly as the parser's
+ *     intermediate representation -- fields, implicit q-monomials, explicit terms
+ *     (product of fields x sum of q-monomials) and noise amplitudes.  This is the
+ *     seam the reference's host classes drive through their extern "C" launchers
+ *     (inc/cupss/field_kernels.cuh:7-19, inc/cupss/term_kernels.cuh:7-15) plus
+ *     cuFFT/cuRAND (src/field.cpp:247-316, src/term.cpp:48-64); here one call
+ *     advances whole time steps.
+ *
+ *  2. Evolver level (cupssgb_evolver_*): the reference's public C++ API
+ *     (inc/cupss/evolver.h:14-86) -- string equations parsed by the library --
+ *     flattened to C for FFI callers (ctypes, cgo, JNI).
+ *
+ * Conventions: every function returns 0 on success or a negative status
+ * (CUPSSGB_ERR_*); cupssgb_last_error() gives the message of the last failure on
+ * the calling thread.  Real fields are sx*sy*sz floats indexed k*sx*sy + j*sx + i
+ * (the reference's index, src/field.cpp:102).  Fourier fields are the reference's
+ * full complex layout: 2*sx*sy*sz floats (re, im) at the same index, unnormalised
+ * forward transform of the real field (cuFFT/FFTW convention).
+ * Grid sizes: powers of two, 2 <= sx <= 2048, 1 <= sy, sz <= 1024.
+ * One CUDA stream per handle; handles are independent and hold no global state.
+ */
+#ifndef CUPSS_GB300_H
+#define CUPSS_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CUPSSGB_OK 0
+#define CUPSSGB_ERR_INVALID (-1)
+#define CUPSSGB_ERR_CUDA (-2)
+#define CUPSSGB_ERR_UNSUPPORTED (-3)
+#define CUPSSGB_ERR_STATE (-4)
+#define CUPSSGB_ERR_PARSE (-5)
+#define CUPSSGB_ERR_LIMIT (-6)
+
+/* Same members and layout as the reference's struct pres (inc/cupss/defines.h:31-39). */
+typedef struct cupssgb_pres {
+  float preFactor;
+  int q2n;
+  int iqx;
+  int iqy;
+  int iqz;
+  int invq;
+} cupssgb_pres;
+
+typedef struct cupssgb_solver cupssgb_solver;
+typedef struct cupssgb_evolver cupssgb_evolver;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* cupssgb_last_error(void);
+/* Library version, major*10000 + minor*100 + patch. */
+int cupssgb_version(void);
+
+/* ---------------- solver level ---------------- */
+
+/* Replaces the per-field/per-term allocation and plan creation of
+ * field::common_constructor / term::common_constructor (src/field_init.cpp:15-154,
+ * src/term_init.cpp:11-71).  dx, dy, dz: cell sizes; dt: time step. */
+int cupssgb_solver_create(int sx, int sy, int sz, float dx, float dy, float dz, float dt,
+                          cupssgb_solver** out);
+int cupssgb_solver_destroy(cupssgb_solver* s);
+
+/* evolver::createField (src/evolver.cpp:177-196).  Returns the field index (>= 0). */
+int cupssgb_solver_add_field(cupssgb_solver* s, int dynamic);
+/* field::implicit as built by parser::add_equation (src/parser.cpp:681-738):
+ * dynamic fields get the LHS prefactors negated, non-dynamic ones as written. */
+int cupssgb_solver_set_implicit(cupssgb_solver* s, int field, const cupssgb_pres* pres, int n);
+/* evolver::createTerm (src/evolver.cpp:326-362): product = field indices
+ * (multiset, n_product >= 0), pres = the term's prefactor list.  Returns the term
+ * index within the field (>= 0). */
+int cupssgb_solver_add_term(cupssgb_solver* s, int field, const int* product, int n_product,
+                            const cupssgb_pres* pres, int n_pres);
+/* field::updateParameter / term::precomputePrefactors (src/field.cpp:422-441,
+ * src/term_init.cpp:135-200): new prefactors for an existing term (same count). */
+int cupssgb_solver_set_term_pres(cupssgb_solver* s, int field, int term, const cupssgb_pres* pres,
+                                 int n);
+/* Implicit prefactors may be replaced after prepare (field::precalculateImplicit). */
+int cupssgb_solver_update_implicit(cupssgb_solver* s, int field, const cupssgb_pres* pres, int n);
+/* evolver::addNoise (src/evolver.cpp:162-171); amp = NULL switches noise off. */
+int cupssgb_solver_set_noise(cupssgb_solver* s, int field, const cupssgb_pres* amp);
+/* Seed of the counter-based noise (the reference seeds cuRAND with time(NULL),
+ * src/field_init.cpp:137). */
+int cupssgb_solver_set_seed(cupssgb_solver* s, unsigned long long seed);
+
+/* Replaces field::prepareDevice + precalculateImplicit + term::prepareDevice
+ * (src/field_init.cpp:215-284, src/term_init.cpp:108-200): compiles the step
+ * plan and allocates device state.  All fields start at zero. */
+int cupssgb_solver_prepare(cupssgb_solver* s);
+/* Initial condition: copyHostToDevice + toComp of evolver::prepareProblem
+ * (src/evolver.cpp:114-117).  host_real: sx*sy*sz floats. */
+int cupssgb_solver_set_real(cupssgb_solver* s, int field, const float* host_real);
+/* Same from a device pointer (stream-ordered on the solver's stream). */
+int cupssgb_solver_set_real_device(cupssgb_solver* s, int field, const float* dev_real);
+/* nsteps x evolver::advanceTime (src/evolver.cpp:199-226), asynchronous. */
+int cupssgb_solver_advance(cupssgb_solver* s, int nsteps);
+/* Real-space field (field::real_array after the last step, src/field.cpp:64-66). */
+int cupssgb_solver_get_real(cupssgb_solver* s, int field, float* host_real);
+int cupssgb_solver_get_real_device(cupssgb_solver* s, int field, float* dev_real);
+/* Fourier-space field (field::comp_array, full complex layout, 2*N floats). */
+int cupssgb_solver_get_fourier(cupssgb_solver* s, int field, float* host_complex);
+int cupssgb_solver_get_fourier_device(cupssgb_solver* s, int field, float* dev_complex);
+/* Waits for all work queued on the solver's stream. */
+int cupssgb_solver_synchronize(cupssgb_solver* s);
+/* Steps taken so far, kernels launched so far, device bytes held. */
+long long cupssgb_solver_step_count(const cupssgb_solver* s);
+long long cupssgb_solver_launch_count(const cupssgb_solver* s);
+long long cupssgb_solver_device_bytes(const cupssgb_solver* s);
+/* The solver's CUDA stream (cudaStream_t), for callers that order their own work. */
+void* cupssgb_solver_stream(const cupssgb_solver* s);
+
+/* ---------------- evolver level ---------------- */
+
+/* evolver(bool with_cuda, sx[, sy[, sz]], dx[, dy[, dz]], dt, writeEvery)
+ * (inc/cupss/evolver.h:31-33).  Pass sy = sz = 1 (and dy = dz = 1) for lower
+ * dimensions.  with_cuda = 0 keeps the host arrays current after every step (the
+ * step itself always runs on the GPU). */
+int cupssgb_evolver_create(int with_cuda, int sx, int sy, int sz, float dx, float dy, float dz,
+                           float dt, int write_every, cupssgb_evolver** out);
+int cupssgb_evolver_destroy(cupssgb_evolver* e);
+/* evolver::createField, addParameter, addEquation, addNoise, updateParameter,
+ * setOutputField (src/evolver.cpp:128-196, 386-394).  Parse errors return
+ * CUPSSGB_ERR_PARSE instead of exiting the process. */
+int cupssgb_evolver_create_field(cupssgb_evolver* e, const char* name, int dynamic);
+int cupssgb_evolver_add_parameter(cupssgb_evolver* e, const char* name, float value);
+int cupssgb_evolver_add_equation(cupssgb_evolver* e, const char* equation);
+int cupssgb_evolver_add_noise(cupssgb_evolver* e, const char* field, const char* amplitude);
+int cupssgb_evolver_update_parameter(cupssgb_evolver* e, const char* name, float value);
+int cupssgb_evolver_set_output_field(cupssgb_evolver* e, const char* field, int output);
+int cupssgb_evolver_set_seed(cupssgb_evolver* e, unsigned long long seed);
+/* Writes field.real_array[i].x for i < N before prepareProblem (fieldsReal). */
+int cupssgb_evolver_set_real(cupssgb_evolver* e, const char* field, const float* host_real);
+/* evolver::prepareProblem (src/evolver.cpp:81-126). */
+int cupssgb_evolver_prepare(cupssgb_evolver* e);
+/* nsteps x evolver::advanceTime, including writeOut every writeEveryNSteps. */
+int cupssgb_evolver_advance(cupssgb_evolver* e, int nsteps);
+/* evolver::writeOut (src/evolver.cpp:228-232). */
+int cupssgb_evolver_write_out(cupssgb_evolver* e);
+/* copyAllDataToHost then field.real_array[.].x / comp_array for one field. */
+int cupssgb_evolver_get_real(cupssgb_evolver* e, const char* field, float* host_real);
+int cupssgb_evolver_get_fourier(cupssgb_evolver* e, const char* field, float* host_complex);
+float cupssgb_evolver_get_parameter(cupssgb_evolver* e, const char* name);
+int cupssgb_evolver_current_step(const cupssgb_evolver* e);
+/* Parsed system as JSON: [{"name", "dynamic", "implicit": [[pre,q2n,iqx,iqy,iqz,invq]..],
+ * "terms": [{"product": [names], "pres": [[..]..]}..], "noisy", "noise": [..]}..].
+ * Returns the full length; writes at most buflen-1 chars plus a NUL. */
+int cupssgb_evolver_describe(const cupssgb_evolver* e, char* buf, int buflen);
+/* The solver behind an evolver (valid after prepare), for device-level access. */
+cupssgb_solver* cupssgb_evolver_solver(cupssgb_evolver* e);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUPSS_GB300_H */

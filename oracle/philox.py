@@ -1,0 +1,101 @@
+"""Oracle restatement of the Fourier-space noise stream (TEST INFRASTRUCTURE ONLY).
+
+Only ``tests/``, ``__graft_entry__.smoke`` and the CPU-baseline leg of ``bench.py``
+may import this module.
+
+The reference (src/field.cpp:300-316, src/field_init.cpp:130-137) draws real
+white N(0,1) noise with cuRAND's Philox4x32-10 generator seeded from
+``time(NULL)`` and forward-FFTs it (unnormalised).  The DFT of i.i.d. N(0,1)
+real noise is a Hermitian complex Gaussian field: each independent pair
+(k, -k) has Re and Im ~ N(0, N/2); self-conjugate bins are real ~ N(0, N).
+The GB300 engine generates that field directly in Fourier space with a
+counter-based Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random
+numbers: as easy as 1, 2, 3", SC'11) and the Box-Muller transform.  This module
+restates the same definition in numpy so tests can feed the oracle the exact
+realisation the GPU used:
+
+  key     = (seed mod 2^32, seed >> 32)
+  counter = (lin, step, field_id, 0)       lin = (kz*sy + ky)*sx + kx  (canonical member)
+  u1 = ((x0 >> 8) + 1) * 2^-24 in (0,1],  u2 = (x1 >> 8) * 2^-24 in [0,1)
+  g1 + i g2 = sqrt(-2 ln u1) * exp(2 pi i u2)
+  value at canonical k = sqrt(N/2) (g1 + i g2); at -k the conjugate;
+  self-conjugate k: sqrt(N) g1.
+  Canonical member of a pair: for 0 < kx < sx/2 the point itself (its partner
+  has kx > sx/2); on the kx = 0 and kx = sx/2 planes the member with the
+  smaller linear index.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+M0 = np.uint64(0xD2511F53)
+M1 = np.uint64(0xCD9E8D57)
+W0 = np.uint32(0x9E3779B9)
+W1 = np.uint32(0xBB67AE85)
+MASK32 = np.uint64(0xFFFFFFFF)
+
+
+def philox4x32_10(c0, c1, c2, c3, k0, k1):
+    """Vectorised Philox4x32 with 10 rounds; all arguments uint32 arrays/scalars."""
+    c0 = np.asarray(c0, np.uint32)
+    c1 = np.asarray(c1, np.uint32)
+    c2 = np.asarray(c2, np.uint32)
+    c3 = np.asarray(c3, np.uint32)
+    k0 = np.uint32(k0)
+    k1 = np.uint32(k1)
+    with np.errstate(over="ignore"):
+        for r in range(10):
+            p0 = c0.astype(np.uint64) * M0
+            p1 = c2.astype(np.uint64) * M1
+            hi0 = (p0 >> np.uint64(32)).astype(np.uint32)
+            lo0 = (p0 & MASK32).astype(np.uint32)
+            hi1 = (p1 >> np.uint64(32)).astype(np.uint32)
+            lo1 = (p1 & MASK32).astype(np.uint32)
+            c0, c1, c2, c3 = hi1 ^ c1 ^ k0, lo1, hi0 ^ c3 ^ k1, lo0
+            k0 = np.uint32(k0 + W0)
+            k1 = np.uint32(k1 + W1)
+    return c0, c1, c2, c3
+
+
+def normal_pair(x0, x1, dtype=np.float64):
+    u1 = (((x0 >> np.uint32(8)).astype(np.float64) + 1.0) * 2.0 ** -24).astype(dtype)
+    u2 = ((x1 >> np.uint32(8)).astype(np.float64) * 2.0 ** -24).astype(dtype)
+    r = np.sqrt(-2.0 * np.log(u1))
+    ang = 2.0 * np.pi * u2
+    return r * np.cos(ang), r * np.sin(ang)
+
+
+def fourier_noise(sx, sy, sz, seed, step, field_id, dtype=np.complex128):
+    """Full (reference-layout, [kz][ky][kx]) Hermitian noise field for one step."""
+    N = sx * sy * sz
+    k0 = np.uint32(seed & 0xFFFFFFFF)
+    k1 = np.uint32((seed >> 32) & 0xFFFFFFFF)
+    kz, ky, kx = np.meshgrid(np.arange(sz), np.arange(sy), np.arange(sx), indexing="ij")
+    pkz = (-kz) % sz
+    pky = (-ky) % sy
+    pkx = (-kx) % sx
+    lin = (kz * sy + ky) * sx + kx
+    plin = (pkz * sy + pky) * sx + pkx
+    edge = (kx == 0) | (2 * kx == sx)
+    self_is_canon = np.where(edge, lin <= plin, 2 * kx < sx)
+    canon = np.where(self_is_canon, lin, plin).astype(np.uint32)
+    x0, x1, _, _ = philox4x32_10(canon, np.uint32(step), np.uint32(field_id), np.uint32(0), k0, k1)
+    g1, g2 = normal_pair(x0, x1)
+    half = np.sqrt(N / 2.0)
+    val = half * (g1 + 1j * g2)
+    val = np.where(self_is_canon, val, np.conj(val))
+    val = np.where(lin == plin, np.sqrt(float(N)) * g1 + 0j, val)
+    return val.astype(dtype)
+
+
+class NoiseProvider:
+    """Callable for ``RefSolver(noise=...)``: (step, field_index) -> noise field."""
+
+    def __init__(self, sx, sy, sz, seed, field_ids=None):
+        self.sx, self.sy, self.sz, self.seed = sx, sy, sz, seed
+        self.field_ids = field_ids
+
+    def __call__(self, step, f):
+        fid = f if self.field_ids is None else self.field_ids[f]
+        return fourier_noise(self.sx, self.sy, self.sz, self.seed, step, fid)
+

@@ -1,0 +1,381 @@
+"""Benchmark of the GB300 pseudospectral step (cuPSS drop-in).
+
+Default workload: 3D Cahn-Hilliard with conserved noise on a 256^3 periodic grid,
+FP32, a=-1, b=1, k=1, dt=0.005, T=0.01, phi0 ~ U[-0.05, 0.05] from SplitMix64
+seed 20261203, equations in reference syntax:
+    dt phi + q^2*(a + k*q^2)*phi = -b*q^2*phi^3      noise "2*T*q^2"
+A bench step is one time step (evolver::advanceTime) of the whole grid; the
+metric is grid-point-steps per second.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Under torchrun (N > 1) every rank advances its own independent replica (a single
+solve does not shard); value = all ranks' point-steps / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "ch3d-256": dict(shape=(256, 256, 256), dt=0.005, params={"a": -1.0, "b": 1.0, "k": 1.0, "T": 0.01},
+                     eqs=["dt phi + q^2*(a + k*q^2)*phi = -b*q^2*phi^3"], noise=[("phi", "2*T*q^2")],
+                     init=(-0.05, 0.05), solve_steps=2000, steps=2000, warmup=20),
+    "ch2d-256": dict(shape=(256, 256, 1), dt=0.01, params={"a": -1.0, "b": 1.0, "k": 1.0},
+                     eqs=["dt phi + q^2*(a + k*q^2)*phi = -b*q^2*phi^3"], noise=[],
+                     init=(-0.1, 0.1), solve_steps=10000, steps=10000, warmup=50),
+}
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM = 6800.0
+
+
+def peak_hbm():
+    try:
+        with open(PEAKS_FILE) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM, "fallback"
+
+
+# --------------------------------------------------------------------------------------
+# clocks sampler (nvidia-smi during the timed region)
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        time.sleep(0.15)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = list(self.rows)
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i] and "Not" not in r[5 + i]})
+        pw = [float(r[3]) for r in rows if r[3].replace(".", "").isdigit()]
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows), "power_w_max": max(pw) if pw else None}
+
+
+# --------------------------------------------------------------------------------------
+def make_evolver(wl, seed=42):
+    import cupss_gb300 as c
+    sx, sy, sz = wl["shape"]
+    e = c.Evolver(True, sx, sy, sz, 1.0, 1.0, 1.0, dt=wl["dt"], write_every=10 ** 9)
+    e.createField("phi", True)
+    for k, v in wl["params"].items():
+        e.addParameter(k, v)
+    for q in wl["eqs"]:
+        e.addEquation(q)
+    for f, a in wl["noise"]:
+        e.addNoise(f, a)
+    e.setNoiseSeed(seed)
+    init = c.splitmix64_uniform(sx * sy * sz, 20261203, *wl["init"])
+    e.setReal("phi", init)
+    e.prepareProblem()
+    return e, init
+
+
+class _SolverView:
+    """Solver-level calls on the solver owned by an Evolver."""
+
+    def __init__(self, handle, shape):
+        from cupss_gb300.api import Solver
+        import cupss_gb300.capi as capi
+        self.lib = capi.load()
+        self.h = handle
+        self.shape = (shape[2], shape[1], shape[0])
+        self.N = shape[0] * shape[1] * shape[2]
+        for name in ("time_advance", "set_kernel_timing", "kernel_report", "set_real_ptr", "get_real_ptr",
+                     "synchronize", "advance"):
+            setattr(self, name, getattr(Solver, name).__get__(self))
+
+    @property
+    def launch_count(self):
+        return self.lib.cupssgb_solver_launch_count(self.h)
+
+
+def kernel_bytes(kind, wl):
+    """Algorithmic bytes per launch of each kernel of the 3D/2D Cahn-Hilliard step.
+    Spectral arrays are packed half spectra: 8 B per complex = 4 B per grid point.
+    Dealiased channels (order 3, |n| <= N/4) are written only where unmasked, at the
+    engine's tile granularity (W columns x line pairs)."""
+    sx, sy, sz = wl["shape"]
+    N = sx * sy * sz
+    arr = 4.0 * N
+    Lx = sx // 2
+    mx = sx // 4
+    if sz > 1:
+        W = 8
+        fx = min(Lx, (mx // W + 1) * W) / Lx
+        fy = min(sy // 2, sy // 4 + 1) / (sy // 2)
+        return {"turnaround_z": 3 * arr + fx * fy * arr,     # read G'', read/write state, write H'
+                "line_inv_y": 2 * fx * arr,                  # read H', write H (unmasked columns)
+                "row_pass": 2 * arr,                         # read H, write G'
+                "line_fwd_y": 2 * arr}[kind]                 # G' -> G''
+    W = 16
+    fx = min(Lx, (mx // W + 1) * W) / Lx
+    return {"turnaround_y": 3 * arr + fx * arr, "row_pass": 2 * arr}[kind]
+
+
+def run_cpu_baseline(wl, steps_budget_s=20.0, max_steps=None, workers=None):
+    """Times the oracle restatement of the reference CPU path (float32, multithreaded
+    scipy FFT, real white noise + FFT like the reference) on a bounded sample."""
+    from oracle.ref_parser import System
+    from oracle.ref_solver import RefSolver
+    from cupss_gb300.workloads import splitmix64_uniform
+    workers = workers or os.cpu_count() or 1
+    sizes = [wl["shape"]]
+    sx, sy, sz = wl["shape"]
+    while sizes[-1][0] > 32:
+        a, b, c = sizes[-1]
+        sizes.append((a // 2, b // 2 if b > 1 else 1, c // 2 if c > 1 else 1))
+
+    def build(shape):
+        s = System()
+        s.create_field("phi", True)
+        for k, v in wl["params"].items():
+            s.add_parameter(k, v)
+        for q in wl["eqs"]:
+            s.add_equation(q)
+        for f, a in wl["noise"]:
+            s.add_noise(f, a)
+        r = RefSolver(s, *shape, dt=wl["dt"], precision="f32", fft_workers=workers)
+        r.set_real("phi", splitmix64_uniform(shape[0] * shape[1] * shape[2], 20261203, *wl["init"]))
+        r.prepare()
+        return r
+
+    # pick the largest sample whose single step fits the budget comfortably
+    chosen = None
+    for shape in sizes[::-1]:
+        r = build(shape)
+        t0 = time.perf_counter()
+        r.advance(1)
+        dt1 = time.perf_counter() - t0
+        chosen = (shape, r, dt1)
+        if dt1 * 8 > steps_budget_s:
+            break
+    shape, r, dt1 = chosen
+    n = max(1, int(steps_budget_s / max(dt1, 1e-6)))
+    if max_steps:
+        n = min(n, max_steps)
+    t0 = time.perf_counter()
+    r.advance(n)
+    el = time.perf_counter() - t0
+    pts = shape[0] * shape[1] * shape[2]
+    return {"value": pts * n / el, "unit": "pt-steps/s", "cores": workers, "kind": "port",
+            "sample": "%d time steps of the same system on a %dx%dx%d grid (float32 oracle restatement of "
+                      "the reference CPU path, scipy.fft with %d threads), %.1f s" % (
+                          n, shape[0], shape[1], shape[2], workers, el)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def reduce_max(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=None)
+    ap.add_argument("--warmup", type=int, default=None)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="ch3d-256", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--profile-steps", type=int, default=100)
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    K = args.steps if args.steps is not None else wl["steps"]
+    W = args.warmup if args.warmup is not None else wl["warmup"]
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    sx, sy, sz = wl["shape"]
+    N = sx * sy * sz
+    cfg = {"workload": "%s: %dx%dx%d Cahn-Hilliard%s, dt=%g, FP32" % (
+        args.workload, sx, sy, sz, " + conserved noise T=0.01" if wl["noise"] else "", wl["dt"]),
+        "grid": [sx, sy, sz], "equation": wl["eqs"][0], "noise": wl["noise"][0][1] if wl["noise"] else None,
+        "full_solve_steps": wl["solve_steps"],
+        "l2": "working set (state x2, dealiased copies, product spectra) larger than the 126 MB L2",
+        "parallelism": "replicas" if ws > 1 else "single GPU"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = run_cpu_baseline(wl, steps_budget_s=max(10.0, min(150.0, 2.0 * (K + W))), max_steps=K + W)
+        line = {"metric": "grid-pt-steps/s", "value": cb["value"], "unit": "pt-steps/s", "n_gpus": ws,
+                "steps": K, "warmup": W, "ms_per_step": 1e3 * N / cb["value"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
+                "impl": "reference", "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": "pt-steps/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import cupss_gb300 as c
+    from cupss_gb300 import build as b
+    b.build()
+    c.api.set_device(local)
+    e, init = make_evolver(wl)
+    sv = _SolverView(c.load().cupssgb_evolver_solver(e.h), wl["shape"])
+    # warmup
+    sv.advance(W)
+    sv.synchronize()
+    barrier(ws)
+    clocks = Clocks(local)
+    clocks.start()
+    l0 = sv.launch_count
+    ms = sv.time_advance(K)
+    launches = sv.launch_count - l0
+    barrier(ws)
+    clk = clocks.stop()
+    ms_max = reduce_max(ms, ws)
+    value = ws * N * K / (ms_max * 1e-3)
+
+    # per-kernel timing pass (CUDA events around every launch on the solver's stream)
+    sv.set_kernel_timing(True)
+    sv.advance(args.profile_steps)
+    rep = sv.kernel_report()
+    sv.set_kernel_timing(False)
+    peak, peak_kind = peak_hbm()
+    per = {}
+    for kind, v in rep.items():
+        avg = v["ms"] / v["launches"]
+        byts = kernel_bytes(kind, wl)
+        per[kind] = {"launches": v["launches"], "avg_us": 1e3 * avg, "share": None,
+                     "alg_bytes": byts, "GBps": byts / (avg * 1e-3) / 1e9}
+    tot = sum(v["ms"] for v in rep.values())
+    for kind in per:
+        per[kind]["share"] = rep[kind]["ms"] / tot
+    dom = max(per, key=lambda k: rep[k]["ms"])
+    d = per[dom]
+    B_alg = 24.0
+    roof = {"bound": "hbm", "kernel": dom, "achieved": d["GBps"], "peak": peak, "unit": "GB/s",
+            "frac": d["GBps"] / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+            "traffic": None, "alg_bytes_per_launch": d["alg_bytes"], "avg_launch_us": d["avg_us"],
+            "kernels": per,
+            "step_model": {"B_alg_per_pt_step": B_alg,
+                           "achieved_GBps": B_alg * value / ws / 1e9,
+                           "frac": B_alg * value / ws / 1e9 / peak}}
+    prof_file = os.path.join(ROOT, "profiles", "ncu_traffic_%s.json" % args.workload)
+    if os.path.exists(prof_file):
+        try:
+            with open(prof_file) as fh:
+                tr = json.load(fh).get(dom)
+            if tr:
+                roof["traffic"] = tr
+        except Exception:
+            pass
+
+    e2e = None
+    if not args.no_e2e:
+        # host-buffer path through the C-ABI: every step uploads the field from pinned
+        # host memory, advances one step and reads the field back
+        pin_in = c.api.PinnedBuffer(N)
+        pin_out = c.api.PinnedBuffer(N)
+        pin_in.array[:] = init
+        sv.synchronize()
+        barrier(ws)
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            sv.set_real_ptr(0, pin_in.ptr)
+            sv.advance(1)
+            sv.get_real_ptr(0, pin_out.ptr)
+            pin_in.array[:] = pin_out.array
+        el = reduce_max(time.perf_counter() - t0, ws)
+        e2e = {"value": ws * N * args.e2e_steps / el, "unit": "pt-steps/s", "h2d_bytes_per_step": 4 * N,
+               "d2h_bytes_per_step": 4 * N, "steps": args.e2e_steps,
+               "path": "cupssgb_solver_set_real + cupssgb_solver_advance(1) + cupssgb_solver_get_real, "
+                       "pinned host buffers"}
+        pin_in.close()
+        pin_out.close()
+        # a whole solve through the reference-facing evolver C-ABI, host in / host out
+        t0 = time.perf_counter()
+        e2 = make_evolver(wl)[0]
+        e2.advanceTime(wl["solve_steps"])
+        out = e2.getReal("phi")
+        el2 = time.perf_counter() - t0
+        e2e["full_solve"] = {"seconds": el2, "steps": wl["solve_steps"],
+                             "value": N * wl["solve_steps"] / el2,
+                             "path": "cupssgb_evolver_create .. prepare .. advance(%d) .. get_real" % wl["solve_steps"],
+                             "finite": bool(np.isfinite(out).all())}
+        e2.close()
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        cpu = run_cpu_baseline(wl)
+
+    if rank == 0:
+        line = {"metric": "grid-pt-steps/s", "value": value, "unit": "pt-steps/s", "n_gpus": ws, "steps": K,
+                "warmup": W, "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic: SplitMix64 seed 20261203 uniform initial "
+                "field, Fourier-space Philox noise seed 42", "config": cfg, "roofline": roof,
+                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk}
+        print(json.dumps(line), flush=True)
+    e.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -88,6 +88,42 @@ class Solver:
         capi.check(self.lib.cupssgb_solver_get_fourier(self.h, f, capi.fptr(out)))
         return (out[0::2] + 1j * out[1::2]).reshape(self.shape)
 
+    def time_advance(self, n):
+        ms = C.c_double()
+        capi.check(self.lib.cupssgb_solver_time_advance(self.h, int(n), C.byref(ms)))
+        return ms.value
+
+    def set_kernel_timing(self, on):
+        capi.check(self.lib.cupssgb_solver_set_kernel_timing(self.h, int(bool(on))))
+
+    def kernel_report(self):
+        n = capi.check(self.lib.cupssgb_solver_kernel_report(self.h, None, 0))
+        buf = C.create_string_buffer(n + 1)
+        self.lib.cupssgb_solver_kernel_report(self.h, buf, n + 1)
+        return json.loads(buf.value.decode())
+
+    def generated_sources(self):
+        out = []
+        i = 0
+        while True:
+            n = self.lib.cupssgb_solver_generated_source(self.h, i, None, 0)
+            if n < 0:
+                break
+            buf = C.create_string_buffer(n + 1)
+            self.lib.cupssgb_solver_generated_source(self.h, i, buf, n + 1)
+            out.append(buf.value.decode())
+            i += 1
+        return out
+
+    def set_generated_programs(self, on):
+        capi.check(self.lib.cupssgb_solver_set_generated_programs(self.h, int(bool(on))))
+
+    def set_real_ptr(self, f, host_ptr):
+        capi.check(self.lib.cupssgb_solver_set_real(self.h, f, C.cast(host_ptr, capi._FP)))
+
+    def get_real_ptr(self, f, host_ptr):
+        capi.check(self.lib.cupssgb_solver_get_real(self.h, f, C.cast(host_ptr, capi._FP)))
+
     @property
     def step_count(self):
         return self.lib.cupssgb_solver_step_count(self.h)
@@ -99,6 +135,37 @@ class Solver:
     @property
     def device_bytes(self):
         return self.lib.cupssgb_solver_device_bytes(self.h)
+
+
+class PinnedBuffer:
+    """Page-locked host buffer (cupssgb_host_alloc) viewed as a float32 numpy array."""
+
+    def __init__(self, nfloats):
+        self.lib = capi.load()
+        p = C.c_void_p()
+        capi.check(self.lib.cupssgb_host_alloc(4 * nfloats, C.byref(p)))
+        self.ptr = p
+        self.array = np.ctypeslib.as_array(C.cast(p, capi._FP), shape=(nfloats,))
+
+    def close(self):
+        if self.ptr:
+            self.lib.cupssgb_host_free(self.ptr)
+            self.ptr = None
+
+
+def jit_check(source):
+    """Compiles a generated kernel source for sm_103a (no GPU needed); returns the
+    cubin size or raises CupssError with the NVRTC log."""
+    lib = capi.load()
+    log = C.create_string_buffer(1 << 16)
+    rc = lib.cupssgb_jit_check(source.encode(), log, len(log))
+    if rc < 0:
+        raise capi.CupssError(rc, log.value.decode())
+    return rc
+
+
+def set_device(dev):
+    capi.check(capi.load().cupssgb_set_device(int(dev)))
 
 
 class Evolver:

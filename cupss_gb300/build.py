@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = [
     "k_line_1024.cu", "k_line_512.cu", "k_line_256.cu", "k_line_128.cu", "k_line_small.cu",
     "k_row.cu", "k_misc.cu",
-    "engine.cpp", "capi.cpp",
+    "engine.cpp", "capi.cpp", "jit.cpp",
     "host_parser.cpp", "host_evolver.cpp", "host_field_term.cpp", "host_init.cpp", "host_utils.cpp",
 ]
 
@@ -33,11 +33,36 @@ def nvcc_path():
     raise RuntimeError("nvcc not found")
 
 
+JIT_HEADERS = ["engine_types.h", "twiddle32.h", "fft.cuh", "philox.cuh", "point_math.cuh",
+               "line_geom.cuh", "turn.cuh"]
+
+
+def write_jit_headers():
+    """Embeds the device headers the runtime-compiled kernels include (jit_headers.inc)."""
+    names, bodies = [], []
+    for h in JIT_HEADERS:
+        with open(os.path.join(CSRC, h)) as fh:
+            body = fh.read()
+        assert ")CUPSSJIT" not in body
+        names.append('"%s"' % h)
+        bodies.append('R"CUPSSJIT(%s)CUPSSJIT"' % body)
+    text = ("// Generated by cupss_gb300/build.py from the device headers -- do not edit.\n"
+            "static const int kJitNumHeaders = %d;\n"
+            "static const char* const kJitHeaderNames[] = {%s};\n"
+            "static const char* const kJitHeaderSources[] = {\n%s};\n") % (
+        len(names), ", ".join(names), ",\n".join(bodies))
+    out = os.path.join(CSRC, "jit_headers.inc")
+    old = open(out).read() if os.path.exists(out) else None
+    if old != text:
+        with open(out, "w") as fh:
+            fh.write(text)
+
+
 def _deps_mtime():
     m = 0.0
     for d in (CSRC, os.path.join(HERE, "..", "include"), os.path.join(HERE, "..", "include", "cupss")):
         for f in os.listdir(d):
-            if f.endswith((".h", ".cuh")):
+            if f.endswith((".h", ".cuh", ".inc")):
                 m = max(m, os.path.getmtime(os.path.join(d, f)))
     return m
 
@@ -57,6 +82,7 @@ def _compile(src, nvcc, hdr_mtime):
 
 def build(verbose=False, jobs=None):
     os.makedirs(BUILD, exist_ok=True)
+    write_jit_headers()
     nvcc = nvcc_path()
     hdr = _deps_mtime()
     jobs = jobs or min(len(SOURCES), max(2, os.cpu_count() or 2))
@@ -70,7 +96,7 @@ def build(verbose=False, jobs=None):
                 print(log)
     newest = max(os.path.getmtime(o) for o in objs)
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
-        cmd = [nvcc, "-shared", *ARCH, "-o", LIB + ".tmp", *objs, "-lcudart"]
+        cmd = [nvcc, "-shared", *ARCH, "-o", LIB + ".tmp", *objs, "-lcudart", "-lnvrtc"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))

@@ -69,6 +69,15 @@ SIGNATURES = {
     "cupssgb_solver_launch_count": (_LL, [_P]),
     "cupssgb_solver_device_bytes": (_LL, [_P]),
     "cupssgb_solver_stream": (_P, [_P]),
+    "cupssgb_solver_time_advance": (_I, [_P, _I, C.POINTER(C.c_double)]),
+    "cupssgb_solver_set_kernel_timing": (_I, [_P, _I]),
+    "cupssgb_solver_kernel_report": (_I, [_P, C.c_char_p, _I]),
+    "cupssgb_solver_generated_source": (_I, [_P, _I, C.c_char_p, _I]),
+    "cupssgb_solver_set_generated_programs": (_I, [_P, _I]),
+    "cupssgb_jit_check": (_I, [C.c_char_p, C.c_char_p, _I]),
+    "cupssgb_host_alloc": (_I, [_LL, C.POINTER(_P)]),
+    "cupssgb_host_free": (_I, [_P]),
+    "cupssgb_set_device": (_I, [_I]),
     "cupssgb_evolver_create": (_I, [_I, _I, _I, _I, _F, _F, _F, _F, _I, C.POINTER(_P)]),
     "cupssgb_evolver_destroy": (_I, [_P]),
     "cupssgb_evolver_create_field": (_I, [_P, _S, _I]),

@@ -9,6 +9,7 @@
 #include "../../include/cupss_gb300.h"
 #include "engine.h"
 #include "host_common.h"
+#include "jit.h"
 
 struct cupssgb_solver {
   cupssgb::Solver* s;
@@ -229,6 +230,95 @@ int cupssgb_solver_synchronize(cupssgb_solver* s) {
     s->s->synchronize();
     return 0;
   });
+}
+
+int cupssgb_solver_time_advance(cupssgb_solver* s, int nsteps, double* ms) {
+  NEED(s);
+  NEED(ms);
+  return guard([&] {
+    *ms = s->s->time_advance(nsteps);
+    return 0;
+  });
+}
+
+int cupssgb_solver_set_kernel_timing(cupssgb_solver* s, int on) {
+  NEED(s);
+  return guard([&] {
+    s->s->set_kernel_timing(on != 0);
+    return 0;
+  });
+}
+
+int cupssgb_solver_kernel_report(cupssgb_solver* s, char* buf, int buflen) {
+  NEED(s);
+  std::string r;
+  int rc = guard([&] {
+    r = s->s->kernel_report();
+    return 0;
+  });
+  if (rc != 0) return rc;
+  if (buf && buflen > 0) {
+    const size_t n = std::min((size_t)buflen - 1, r.size());
+    std::memcpy(buf, r.data(), n);
+    buf[n] = 0;
+  }
+  return (int)r.size();
+}
+
+int cupssgb_solver_generated_source(cupssgb_solver* s, int index, char* buf, int buflen) {
+  NEED(s);
+  std::string src;
+  int rc = guard([&] {
+    std::vector<std::string> v = s->s->generated_sources();
+    if (index < 0 || index >= (int)v.size()) return fail(CUPSSGB_ERR_INVALID, "no such generated program");
+    src = v[index];
+    return 0;
+  });
+  if (rc != 0) return rc;
+  if (buf && buflen > 0) {
+    const size_t n = std::min((size_t)buflen - 1, src.size());
+    std::memcpy(buf, src.data(), n);
+    buf[n] = 0;
+  }
+  return (int)src.size();
+}
+
+int cupssgb_solver_set_generated_programs(cupssgb_solver* s, int on) {
+  NEED(s);
+  s->s->set_use_jit(on != 0);
+  return 0;
+}
+
+int cupssgb_jit_check(const char* source, char* log, int loglen) {
+  NEED(source);
+  std::string msg;
+  int rc = guard([&] {
+    size_t bytes = 0;
+    msg = cupssgb::jit_compile_only(source, &bytes);
+    return msg.empty() ? (int)bytes : fail(CUPSSGB_ERR_CUDA, "NVRTC compilation failed");
+  });
+  if (log && loglen > 0) {
+    const size_t n = std::min((size_t)loglen - 1, msg.size());
+    std::memcpy(log, msg.data(), n);
+    log[n] = 0;
+  }
+  return rc;
+}
+
+int cupssgb_host_alloc(long long bytes, void** out) {
+  NEED(out);
+  cudaError_t e = cudaMallocHost(out, (size_t)bytes);
+  return e == cudaSuccess ? 0 : fail(CUPSSGB_ERR_CUDA, cudaGetErrorString(e));
+}
+
+int cupssgb_host_free(void* p) {
+  cudaError_t e = cudaFreeHost(p);
+  return e == cudaSuccess ? 0 : fail(CUPSSGB_ERR_CUDA, cudaGetErrorString(e));
+}
+
+int cupssgb_set_device(int device) {
+  cudaError_t e = cudaSetDevice(device);
+  return e == cudaSuccess ? 0 : fail(CUPSSGB_ERR_CUDA, cudaGetErrorString(e));
 }
 
 long long cupssgb_solver_step_count(const cupssgb_solver* s) { return s ? s->s->step_count() : -1; }

@@ -3,10 +3,12 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <sstream>
 
+#include "jit.h"
 #include "launch.h"
 
 namespace cupssgb {
@@ -25,6 +27,8 @@ std::string cuda_msg(cudaError_t e, const char* what) {
 
 Solver::Solver(int sx, int sy, int sz, float dx, float dy, float dz, float dt)
     : sx_(sx), sy_(sy), sz_(sz), dx_(dx), dy_(dy), dz_(dz), dt_(dt) {
+  const char* jit = std::getenv("CUPSSGB_JIT");
+  use_jit_ = !(jit && std::string(jit) == "0");
   if (!pow2(sx) || sx < 2 || sx > 2048 || !pow2(sy) || sy > 1024 || !pow2(sz) || sz > 1024)
     throw Error(kErrUnsupported,
                 "grid sizes must be powers of two: 2 <= sx <= 2048, 1 <= sy, sz <= 1024");
@@ -39,6 +43,7 @@ Solver::Solver(int sx, int sy, int sz, float dx, float dy, float dz, float dt)
 
 Solver::~Solver() {
   if (stream_) cudaStreamSynchronize(stream_);
+  for (cudaEvent_t e : ev_pool_) cudaEventDestroy(e);
   for (void* p : allocs_) cudaFree(p);
   if (stream_) cudaStreamDestroy(stream_);
 }
@@ -194,13 +199,26 @@ void Solver::prepare() {
   scratch_spec_ = (float2*)dalloc(half * sizeof(float2));
   check(cudaStreamSynchronize(stream_), "prepare sync");
   prepared_ = true;
+  if (use_jit_) {
+    // compile the specialised update programs now, not inside the first step
+    const int L = (dim_ == 3) ? sz_ : sy_;
+    const int nl = (dim_ == 3) ? 2 : 1;
+    for (Phase& P : phases_) {
+      if (P.fields.empty()) continue;
+      LineParams p;
+      int nslots = 0;
+      bool any_chan = false;
+      fill_turn(P, p, nslots, any_chan);
+      jit_kernel(turn_source(P, p, L, nl), "cupssgb_turn");
+    }
+  }
 }
 
 int Solver::pick_w(int L, int nl, int nslots) const {
   int W = 16;
   while (W > Lx_) W /= 2;
   if (W < 1) W = 1;
-  while (W > 1 && (line_threads(L, nl, W) > 512 ||
+  while (W > 1 && (line_threads(L, nl, W) > 256 ||
                    line_pass_smem(L, nl, W, std::max(nslots, 1)) > 200 * 1024))
     W /= 2;
   if (line_pass_smem(L, nl, W, std::max(nslots, 1)) > 220 * 1024)
@@ -352,58 +370,27 @@ void Solver::synchronize() {
   if (stream_) check(cudaStreamSynchronize(stream_), "synchronize");
 }
 
-void Solver::run_phase(Phase& P) {
-  if (P.fields.empty()) return;
-  // ---- row pass: real-space products of the dealiased copies ----
-  if (!P.products.empty()) {
-    XParams x;
-    std::memset(&x, 0, sizeof(x));
-    x.Lx = Lx_;
-    x.rows = sy_ * sz_;
-    x.in_mode = kXInSpectral;
-    x.out_mode = kXOutSpectral;
-    x.out_scale = 1.f;
-    x.n_in = (int)P.xin.size();
-    for (int i = 0; i < x.n_in; ++i) x.in[i] = chan_[P.xin[i]];
-    x.n_prod = (int)P.products.size();
-    for (int q = 0; q < x.n_prod; ++q) {
-      x.out[q] = P.prodbuf[q];
-      x.prod_n[q] = (int)P.products[q].size();
-      for (int t = 0; t < x.prod_n[q]; ++t) {
-        const int g = P.products[q][t];
-        x.prod_f[q][t] = (int)(std::find(P.xin.begin(), P.xin.end(), g) - P.xin.begin());
-      }
-    }
-    x.tw = tw_;
-    check(launch_row_pass(x, stream_), "row pass");
-    ++launches_;
-    if (dim_ == 3) {
-      for (size_t q = 0; q < P.products.size(); ++q)
-        line_fwd_inv(kGeoY3, kModeFwd, P.prodbuf[q], P.prodbuf[q], Lx_);
-    }
-  }
-  // ---- turnaround ----
+void Solver::fill_turn(const Phase& P, LineParams& p, int& nslots, bool& any_chan) const {
   const int geo = (dim_ == 3) ? kGeoZ3 : kGeoCol;
   const int L = (dim_ == 3) ? sz_ : sy_;
-  const int nl = (dim_ == 3) ? 2 : 1;
-  LineParams p;
+  const bool have_dev = prepared_;
+  any_chan = false;
   fill_line_common(p, L, geo, kModeTurn);
   p.n_prod = (int)P.products.size();
-  for (int q = 0; q < p.n_prod; ++q) p.prod_in[q] = P.prodbuf[q];
-  for (int g = 0; g < nfields(); ++g) p.state[g] = state_[par_[g]][g];
+  for (int q = 0; q < p.n_prod; ++q) p.prod_in[q] = have_dev ? P.prodbuf[q] : nullptr;
+  for (int g = 0; g < nfields(); ++g) p.state[g] = (have_dev ? state_[par_[g]][g] : nullptr);
   p.key0 = (uint32_t)(seed_ & 0xffffffffu);
   p.key1 = (uint32_t)(seed_ >> 32);
   p.step = (uint32_t)step_;
   p.nf = (int)P.fields.size();
   int nt = 0, npres = 0, ts = 0;
-  bool any_chan = false;
   for (int fi = 0; fi < p.nf; ++fi) {
     const int f = P.fields[fi];
     const HostField& hf = fields_[f];
     FieldK& K = p.f[fi];
-    K.cur = state_[par_[f]][f];
-    K.next = state_[par_[f] ^ 1][f];
-    K.chan = (alias_order_[f] > 1) ? (dim_ == 3 ? chanz_[f] : chan_[f]) : nullptr;
+    K.cur = have_dev ? state_[par_[f]][f] : nullptr;
+    K.next = have_dev ? state_[par_[f] ^ 1][f] : nullptr;
+    K.chan = (alias_order_[f] > 1) ? (have_dev ? (dim_ == 3 ? chanz_[f] : chan_[f]) : (float2*)&p) : nullptr;
     any_chan = any_chan || (K.chan != nullptr);
     K.dynamic = hf.dynamic ? 1 : 0;
     K.noisy = hf.noisy ? 1 : 0;
@@ -411,8 +398,21 @@ void Solver::run_phase(Phase& P) {
     K.fid = f;
     K.chan_xlimit = sx_ / (K.order + 1);
     K.chan_ylimit = sy_ / (K.order + 1);
+    K.chan_zlimit = sz_ / (K.order + 1);
     K.term0 = nt;
     K.nterms = (int)hf.terms.size();
+    // states this field's update reads: its own (dynamic, or non-dynamic without terms)
+    // and the sources of its single-field terms, each prefetched into one slot
+    K.nsrc = 0;
+    K.self_src = -1;
+    auto src_slot = [&](int g) {
+      for (int j = 0; j < K.nsrc; ++j)
+        if (K.src[j] == g) return j;
+      if (K.nsrc >= kMaxSrc) throw Error(kErrLimit, "a field reads too many other fields");
+      K.src[K.nsrc] = g;
+      return K.nsrc++;
+    };
+    if (hf.dynamic || hf.terms.empty()) K.self_src = src_slot(f);
     for (size_t t = 0; t < hf.terms.size(); ++t, ++ts) {
       const HostTerm& ht = hf.terms[t];
       TermK& T = p.term[nt++];
@@ -421,7 +421,7 @@ void Solver::run_phase(Phase& P) {
         T.src = 0;
       } else if (ht.product.size() == 1) {
         T.kind = kTermSingle;
-        T.src = ht.product[0];
+        T.src = src_slot(ht.product[0]);
       } else {
         T.kind = kTermProduct;
         T.src = P.term_slot[ts];
@@ -466,16 +466,199 @@ void Solver::run_phase(Phase& P) {
       K.noise_invq = hf.noise.invq;
     }
   }
-  const int nslots = p.n_prod + (any_chan ? 1 : 0);
+  int max_src = 0;
+  for (int fi = 0; fi < p.nf; ++fi) max_src = std::max(max_src, p.f[fi].nsrc);
+  p.src_slots = max_src;
+  nslots = p.n_prod + max_src + (any_chan ? 1 : 0);
+}
+
+const std::string& Solver::turn_source(Phase& P, const LineParams& p, int L, int nl) {
+  std::vector<int> sig = {L, nl, p.nf, p.n_prod};
+  for (int fi = 0; fi < p.nf; ++fi) {
+    const FieldK& K = p.f[fi];
+    sig.insert(sig.end(), {K.dynamic, K.noisy, K.nterms, K.term0, K.nimp, K.imp0, K.noise_q2n, K.noise_invq,
+                           K.self_src, K.nsrc});
+  }
+  int np = 0;
+  for (int t = 0; t < kMaxTerms; ++t) {
+    const TermK& T = p.term[t];
+    sig.insert(sig.end(), {T.kind, T.src, T.s, T.npres, T.pres0});
+    np = std::max(np, T.pres0 + T.npres);
+  }
+  for (int fi = 0; fi < p.nf; ++fi) np = std::max(np, p.f[fi].imp0 + p.f[fi].nimp);
+  for (int j = 0; j < np; ++j) {
+    const PresK& q = p.pres[j];
+    sig.insert(sig.end(), {q.q2n, q.iqx, q.iqy, q.iqz, q.invq});
+  }
+  if (sig != P.jit_sig) {
+    P.jit_sig = sig;
+    P.jit_src = jit_generate_turn(p, L, nl);
+  }
+  return P.jit_src;
+}
+
+std::vector<std::string> Solver::generated_sources() {
+  if (!prepared_) build_plan();
+  std::vector<std::string> out;
+  const int L = (dim_ == 3) ? sz_ : sy_;
+  const int nl = (dim_ == 3) ? 2 : 1;
+  for (Phase& P : phases_) {
+    if (P.fields.empty()) continue;
+    LineParams p;
+    int nslots = 0;
+    bool any_chan = false;
+    fill_turn(P, p, nslots, any_chan);
+    out.push_back(jit_generate_turn(p, L, nl));
+  }
+  return out;
+}
+
+void Solver::run_phase(Phase& P) {
+  if (P.fields.empty()) return;
+  // ---- row pass: real-space products of the dealiased copies ----
+  if (!P.products.empty()) {
+    XParams x;
+    std::memset(&x, 0, sizeof(x));
+    x.Lx = Lx_;
+    x.rows = sy_ * sz_;
+    x.in_mode = kXInSpectral;
+    x.out_mode = kXOutSpectral;
+    x.out_scale = 1.f;
+    x.n_in = (int)P.xin.size();
+    for (int i = 0; i < x.n_in; ++i) x.in[i] = chan_[P.xin[i]];
+    x.n_prod = (int)P.products.size();
+    for (int q = 0; q < x.n_prod; ++q) {
+      x.out[q] = P.prodbuf[q];
+      x.prod_n[q] = (int)P.products[q].size();
+      for (int t = 0; t < x.prod_n[q]; ++t) {
+        const int g = P.products[q][t];
+        x.prod_f[q][t] = (int)(std::find(P.xin.begin(), P.xin.end(), g) - P.xin.begin());
+      }
+    }
+    x.tw = tw_;
+    mark_begin();
+    check(launch_row_pass(x, stream_), "row pass");
+    mark_end("row_pass");
+    ++launches_;
+    if (dim_ == 3) {
+      for (size_t q = 0; q < P.products.size(); ++q) {
+        mark_begin();
+        line_fwd_inv(kGeoY3, kModeFwd, P.prodbuf[q], P.prodbuf[q], Lx_);
+        mark_end("line_fwd_y");
+      }
+    }
+  }
+  // ---- turnaround ----
+  const int geo = (dim_ == 3) ? kGeoZ3 : kGeoCol;
+  const int L = (dim_ == 3) ? sz_ : sy_;
+  const int nl = (dim_ == 3) ? 2 : 1;
+  LineParams p;
+  int nslots = 0;
+  bool any_chan = false;
+  fill_turn(P, p, nslots, any_chan);
   p.W = pick_w(L, nl, nslots);
   dim3 grid((Lx_ + p.W - 1) / p.W, dim_ == 3 ? std::max(sy_ / 2, 1) : 1);
-  check(launch_line_pass(p, nl, nslots, grid, stream_), "turnaround");
+  mark_begin();
+  if (use_jit_) {
+    const std::string& src = turn_source(P, p, L, nl);
+    cudaKernel_t k = jit_kernel(src, "cupssgb_turn");
+    dim3 block(p.W, line_threads(L, 1, 1), nl);
+    void* args[] = {(void*)&p};
+    check(cudaLaunchKernel((const void*)k, grid, block, args, line_pass_smem(L, nl, p.W, nslots), stream_),
+          "turnaround (generated)");
+  } else {
+    check(launch_line_pass(p, nl, nslots, grid, stream_), "turnaround");
+  }
+  mark_end(dim_ == 3 ? "turnaround_z" : "turnaround_y");
   ++launches_;
   for (int f : P.fields) par_[f] ^= 1;
   if (dim_ == 3 && any_chan) {
     for (int f : P.fields)
-      if (alias_order_[f] > 1) line_fwd_inv(kGeoY3, kModeInv, chanz_[f], chan_[f], sx_ / (alias_order_[f] + 1));
+      if (alias_order_[f] > 1) {
+        mark_begin();
+        line_fwd_inv(kGeoY3, kModeInv, chanz_[f], chan_[f], sx_ / (alias_order_[f] + 1));
+        mark_end("line_inv_y");
+      }
   }
+}
+
+void Solver::mark_begin() {
+  if (!timing_) return;
+  if (ev_used_ + 2 > ev_pool_.size()) {
+    for (int i = 0; i < 64; ++i) {
+      cudaEvent_t e;
+      check(cudaEventCreate(&e), "cudaEventCreate");
+      ev_pool_.push_back(e);
+    }
+  }
+  check(cudaEventRecord(ev_pool_[ev_used_], stream_), "cudaEventRecord");
+  ev_marks_.push_back({std::string(), ev_used_});
+  ev_used_ += 2;
+}
+
+void Solver::mark_end(const char* kind) {
+  if (!timing_) return;
+  const size_t b = ev_marks_.back().second;
+  ev_marks_.back().first = kind;
+  check(cudaEventRecord(ev_pool_[b + 1], stream_), "cudaEventRecord");
+  if (ev_used_ + 2 > 4096) flush_timing();
+}
+
+void Solver::flush_timing() {
+  if (ev_marks_.empty()) return;
+  check(cudaStreamSynchronize(stream_), "timing sync");
+  for (const auto& mk : ev_marks_) {
+    float ms = 0.f;
+    check(cudaEventElapsedTime(&ms, ev_pool_[mk.second], ev_pool_[mk.second + 1]), "cudaEventElapsedTime");
+    bool found = false;
+    for (auto& kt : ktimes_)
+      if (kt.first == mk.first) {
+        kt.second.first += 1;
+        kt.second.second += ms;
+        found = true;
+      }
+    if (!found) ktimes_.push_back({mk.first, {1, (double)ms}});
+  }
+  ev_marks_.clear();
+  ev_used_ = 0;
+}
+
+void Solver::set_kernel_timing(bool on) {
+  if (timing_ && !on) flush_timing();
+  timing_ = on;
+  if (on) {
+    ktimes_.clear();
+    ev_marks_.clear();
+    ev_used_ = 0;
+  }
+}
+
+std::string Solver::kernel_report() {
+  flush_timing();
+  std::ostringstream os;
+  os << "{";
+  for (size_t i = 0; i < ktimes_.size(); ++i) {
+    if (i) os << ", ";
+    os << "\"" << ktimes_[i].first << "\": {\"launches\": " << ktimes_[i].second.first
+       << ", \"ms\": " << ktimes_[i].second.second << "}";
+  }
+  os << "}";
+  return os.str();
+}
+
+double Solver::time_advance(int nsteps) {
+  cudaEvent_t a, b;
+  check(cudaEventCreate(&a), "cudaEventCreate");
+  check(cudaEventCreate(&b), "cudaEventCreate");
+  check(cudaEventRecord(a, stream_), "cudaEventRecord");
+  advance(nsteps);
+  check(cudaEventRecord(b, stream_), "cudaEventRecord");
+  check(cudaEventSynchronize(b), "cudaEventSynchronize");
+  float ms = 0.f;
+  check(cudaEventElapsedTime(&ms, a, b), "cudaEventElapsedTime");
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ms;
 }
 
 void Solver::advance(int nsteps) {

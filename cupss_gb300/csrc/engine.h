@@ -74,6 +74,16 @@ class Solver {
   void get_fourier(int f, float2* dst, bool dst_on_device);
   void get_real_pairs_device(int f, float2* dst);   // reference float2 layout (x, 0)
   void synchronize();
+  // Kernel timing: when on, every launch of advance() is bracketed by CUDA events on
+  // the solver's stream and its duration is accumulated per kernel kind.
+  void set_kernel_timing(bool on);
+  std::string kernel_report();   // JSON {kind: {"launches": n, "ms": t}}
+  double time_advance(int nsteps);   // advance + CUDA-event elapsed ms on the stream
+  // CUDA sources of the specialised turnaround kernels (one per non-empty phase);
+  // needs no GPU (the plan is built if prepare has not run).
+  std::vector<std::string> generated_sources();
+  void set_use_jit(bool on) { use_jit_ = on; }
+  bool use_jit() const { return use_jit_; }
 
   int sx() const { return sx_; }
   int sy() const { return sy_; }
@@ -96,16 +106,23 @@ class Solver {
     std::vector<int> xin;                    // fields feeding the row pass
     std::vector<float2*> prodbuf;
     std::vector<int> term_slot;              // per (field, term) flattened: product slot or -1
+    std::vector<int> jit_sig;                // structure of the last generated update program
+    std::string jit_src;
   };
 
   void check(cudaError_t e, const char* what);
   void* dalloc(size_t bytes);
   void build_plan();
   void run_phase(Phase& ph);
+  void fill_turn(const Phase& P, LineParams& p, int& nslots, bool& any_chan) const;
+  const std::string& turn_source(Phase& P, const LineParams& p, int L, int nl);
   void fill_line_common(LineParams& p, int L, int geo, int mode) const;
   int pick_w(int L, int nl, int nslots) const;
   void line_fwd_inv(int geo, int mode, const float2* in, float2* out, int xlimit);
   void to_real_scratch(int f);
+  void mark_begin();
+  void mark_end(const char* kind);
+  void flush_timing();
 
   int sx_, sy_, sz_, dim_, Lx_;
   float dx_, dy_, dz_, dt_;
@@ -114,6 +131,7 @@ class Solver {
   std::vector<HostField> fields_;
   std::vector<int> alias_order_;
   bool prepared_ = false;
+  bool use_jit_ = true;
   long long step_ = 0;
   long long launches_ = 0;
   size_t dev_bytes_ = 0;
@@ -129,6 +147,12 @@ class Solver {
   float2* scratch_full_ = nullptr;   // reference-layout full spectrum, allocated on first use
   std::vector<void*> allocs_;
   Phase phases_[2];              // 0: non-dynamic, 1: dynamic
+  // kernel timing
+  bool timing_ = false;
+  std::vector<cudaEvent_t> ev_pool_;
+  size_t ev_used_ = 0;
+  std::vector<std::pair<std::string, size_t>> ev_marks_;   // kind, index of begin event
+  std::vector<std::pair<std::string, std::pair<long long, double>>> ktimes_;
 };
 
 }  // namespace cupssgb

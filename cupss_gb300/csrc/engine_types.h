@@ -9,8 +9,12 @@
 // This is the same information as the reference's full C2C float2 array after its
 // per-step projection onto real fields (src/field.cpp:63-89), in half the bytes.
 #pragma once
+#if defined(__CUDACC_RTC__)
+typedef unsigned int uint32_t;
+#else
 #include <cstdint>
 #include <cuda_runtime.h>
+#endif
 
 namespace cupssgb {
 
@@ -21,6 +25,7 @@ constexpr int kMaxPhaseFields = 12;
 constexpr int kMaxTerms = 24;
 constexpr int kMaxPres = 48;
 constexpr int kMaxFields = 32;
+constexpr int kMaxSrc = 4;         // prefetched state sources of one field's update
 
 // One q-monomial: pre * q^(2 q2n) * qx^iqx * qy^iqy * qz^iqz * |q|^-invq.
 // For explicit terms `pre` already carries the reference's sign rule
@@ -34,7 +39,7 @@ enum TermKind : int { kTermSingle = 0, kTermProduct = 1, kTermConst = 2 };
 
 struct TermK {
   int kind;    // TermKind
-  int src;     // field index (single) or product slot (product)
+  int src;     // prefetch slot of the source state (single) or product slot (product)
   int s;       // 1 -> multiply by i (odd number of iq factors in the first pres)
   int npres, pres0;
 };
@@ -52,6 +57,10 @@ struct FieldK {
   int noise_q2n, noise_invq;
   int chan_xlimit;       // last kx' column with unmasked content (sx/(order+1))
   int chan_ylimit;       // |n_y| limit (sy/(order+1)), used to skip empty 3D tiles
+  int chan_zlimit;       // |n_z| limit (sz/(order+1))
+  int nsrc;              // states prefetched into shared memory for this field
+  int src[kMaxSrc];      // their field indices (own state included when read)
+  int self_src;          // prefetch slot of the own state, or -1
 };
 
 enum LineGeo : int {
@@ -66,6 +75,7 @@ struct LineParams {
   int sx, sy, sz, Lx, L;
   int geo, mode, W;
   float stepqx, stepqy, stepqz, dt, invN, sqrtN, sqrtHalfN;
+  int src_slots;                    // turnaround: shared-memory slots for prefetched states
   // products (turnaround) or channels to transform (fwd/inv passes)
   int n_prod;
   const float2* prod_in[kMaxProd];

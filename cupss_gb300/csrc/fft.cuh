@@ -18,8 +18,9 @@
 // is the standard Cooley-Tukey factorisation; the register DFTs are recursive
 // radix-2 decimation in time with compile-time twiddles.
 #pragma once
+#if !defined(__CUDACC_RTC__)
 #include <cuda_runtime.h>
-#include <utility>
+#endif
 #include "twiddle32.h"
 
 #if defined(__CUDACC__)
@@ -29,6 +30,18 @@
 #endif
 
 namespace cupssgb {
+
+// compile-time index sequence (no <utility> under NVRTC)
+template <int... K>
+struct iseq {};
+template <int N, int... K>
+struct make_iseq_t : make_iseq_t<N - 1, N - 1, K...> {};
+template <int... K>
+struct make_iseq_t<0, K...> {
+  using type = iseq<K...>;
+};
+template <int N>
+using make_iseq = typename make_iseq_t<N>::type;
 
 CG_HD float2 c_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 CG_HD float2 c_sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
@@ -68,7 +81,7 @@ CG_HD float2 tw_const(float2 a) {
 template <int N, bool INV, int S>
 struct Dft {
   template <int O, int K0, int... K>
-  CG_HD static void combine(float2* v, std::integer_sequence<int, K0, K...>) {
+  CG_HD static void combine(float2* v, iseq<K0, K...>) {
     constexpr int H = N / 2;
     float2 ev[H];
 #pragma unroll
@@ -92,7 +105,7 @@ struct Dft {
     } else {
       Dft<N / 2, INV, 2 * S>::template run<O>(v);
       Dft<N / 2, INV, 2 * S>::template run<O + S>(v);
-      combine<O>(v, std::make_integer_sequence<int, N / 2>{});
+      combine<O>(v, make_iseq<N / 2>{});
     }
   }
 };

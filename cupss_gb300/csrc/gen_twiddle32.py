@@ -19,9 +19,9 @@ lines = ["// Generated by gen_twiddle32.py -- do not edit.",
          "#pragma once",
          "namespace cupssgb {",
          "// kTw32Re[j] + i*kTw32Im[j] = exp(-2*pi*i*j/32)",
-         "__host__ __device__ constexpr float kTw32Re[32] = {"]
+         "constexpr float kTw32Re[32] = {"]
 lines.append(", ".join(f32hex(math.cos(2 * math.pi * j / 32)) for j in range(32)) + "};")
-lines.append("__host__ __device__ constexpr float kTw32Im[32] = {")
+lines.append("constexpr float kTw32Im[32] = {")
 lines.append(", ".join(f32hex(-math.sin(2 * math.pi * j / 32)) for j in range(32)) + "};")
 lines.append("}  // namespace cupssgb")
 here = os.path.dirname(os.path.abspath(__file__))

@@ -1,0 +1,198 @@
+// Runtime specialisation of the turnaround kernel (NVRTC).
+//
+// The update program of a phase -- which fields, which terms (product / single field /
+// constant), which q-monomials with which exponents, implicit and noise structure --
+// is fixed once the equations are parsed.  The engine emits it as straight-line CUDA
+// (numerical prefactor values stay in the kernel parameter block, so updateParameter
+// needs no recompilation), compiles it for the running GPU with NVRTC and launches the
+// cubin through the runtime's library API.  Compiled kernels are cached per process by
+// source text.
+#include "jit.h"
+
+#include <nvrtc.h>
+
+#include <map>
+#include <mutex>
+#include <sstream>
+#include <vector>
+
+#include "engine.h"
+#include "jit_headers.inc"
+
+namespace cupssgb {
+
+namespace {
+
+std::mutex g_mu;
+std::map<std::string, cudaKernel_t> g_cache;
+
+std::string pow_expr(const char* base, int n) {
+  if (n <= 0) return "";
+  std::string s;
+  for (int i = 0; i < n; ++i) s += std::string(i ? "*" : "") + base;
+  return "*(" + s + ")";
+}
+
+// keep-test of one prefactor on the half spectrum (see term_mult in point_math.cuh)
+std::string keep_expr(int s, const PresK& p, bool* never) {
+  const int a = p.iqx & 1, b = p.iqy & 1, c = p.iqz & 1;
+  *never = false;
+  if (!a && !b && !c) {
+    if (s & 1) *never = true;
+    return "";
+  }
+  std::ostringstream os;
+  os << "(((" << (s & 1);
+  if (a) os << " ^ (vp.nyx ? 0 : 1)";
+  if (b) os << " ^ (vp.nyy ? 0 : 1)";
+  if (c) os << " ^ (vp.nyz ? 0 : 1)";
+  os << ") & 1) == 0)";
+  return os.str();
+}
+
+}  // namespace
+
+std::string jit_generate_turn(const LineParams& p, int L, int NL) {
+  std::ostringstream o;
+  o << "#include \"turn.cuh\"\n"
+    << "namespace cupssgb {\n"
+    << "struct GenProg {\n"
+    << "  static constexpr bool kUnroll = true;\n"
+    << "  template <class F>\n"
+    << "  __device__ __forceinline__ static float2 eval(const LineParams& P, int fi, const VPoint& vp, "
+       "const F& fx) {\n"
+    << "    const float q2 = vp.q2;\n"
+    << "    switch (fi) {\n";
+  for (int fi = 0; fi < p.nf; ++fi) {
+    const FieldK& K = p.f[fi];
+    bool need_iq = false, need_iqd = false;
+    for (int t = 0; t < K.nterms; ++t) {
+      const TermK& T = p.term[K.term0 + t];
+      for (int j = 0; j < T.npres; ++j) need_iq |= p.pres[T.pres0 + j].invq > 0;
+    }
+    if (K.noisy && K.noise_invq) need_iq = true;
+    for (int j = 0; j < K.nimp; ++j)
+      if (p.pres[K.imp0 + j].invq != 0) (K.dynamic ? need_iqd : need_iq) = true;
+    o << "      case " << fi << ": {\n";
+    if (need_iq) o << "        const float iq = vp.origin ? 0.f : 1.0f / sqrtf(q2);\n";
+    if (need_iqd) o << "        const float iqd = (vp.kx > 0 || vp.ky > 0) ? 1.0f / sqrtf(q2) : 0.f;\n";
+    o << "        float2 acc = make_float2(0.f, 0.f);\n";
+    for (int t = 0; t < K.nterms; ++t) {
+      const TermK& T = p.term[K.term0 + t];
+      o << "        {\n          float mt = 0.f;\n";
+      for (int j = 0; j < T.npres; ++j) {
+        const PresK& pr = p.pres[T.pres0 + j];
+        bool never = false;
+        const std::string keep = keep_expr(T.s, pr, &never);
+        if (never) continue;
+        std::ostringstream term;
+        term << "P.pres[" << T.pres0 + j << "].pre" << pow_expr("q2", pr.q2n) << pow_expr("vp.qx", pr.iqx)
+             << pow_expr("vp.qy", pr.iqy) << pow_expr("vp.qz", pr.iqz) << pow_expr("iq", pr.invq);
+        if (keep.empty()) o << "          mt += " << term.str() << ";\n";
+        else o << "          if " << keep << " mt += " << term.str() << ";\n";
+      }
+      if (T.kind == kTermProduct) o << "          const float2 src = fx.prod(" << T.src << ");\n";
+      else if (T.kind == kTermSingle) o << "          const float2 src = fx.src(" << T.src << ");\n";
+      else
+        o << "          const float2 src = vp.origin ? make_float2((float)P.sx * (float)P.sy * (float)P.sz, "
+             "0.f) : make_float2(0.f, 0.f);\n";
+      o << "          float2 c = c_scale(src, mt);\n";
+      if (T.s) o << "          c = c_muli(c);\n";
+      o << "          acc = c_add(acc, c);\n        }\n";
+    }
+    std::ostringstream amp;
+    if (K.noisy) {
+      amp << "P.f[" << fi << "].noise_base";
+      if (K.noise_q2n) amp << "*sqrtf(1.f" << pow_expr("q2", K.noise_q2n) << ")";
+      if (K.noise_invq) amp << "*sqrtf(1.f" << pow_expr("iq", K.noise_invq) << ")";
+    }
+    const std::string noise = "fx.xi";
+    std::ostringstream imp;
+    for (int j = 0; j < K.nimp; ++j) {
+      const PresK& pr = p.pres[K.imp0 + j];
+      imp << (j ? " + " : "") << "P.pres[" << K.imp0 + j << "].pre" << pow_expr("q2", pr.q2n)
+          << pow_expr(K.dynamic ? "iqd" : "iq", pr.invq);
+    }
+    if (K.dynamic) {
+      o << "        float2 nv = c_add(fx.src(" << K.self_src << "), c_scale(acc, P.dt));\n";
+      if (K.noisy) o << "        nv = c_add(nv, c_scale(" << noise << ", " << amp.str() << "));\n";
+      if (K.nimp > 0)
+        o << "        { const float rd = 1.0f / (1.f - P.dt * (" << imp.str()
+          << ")); nv = make_float2(nv.x * rd, nv.y * rd); }\n";
+    } else {
+      if (K.nterms > 0) o << "        float2 nv = acc;\n";
+      else o << "        float2 nv = fx.src(" << K.self_src << ");\n";
+      if (K.noisy) {
+        if (K.nterms > 0) o << "        nv = c_add(nv, c_scale(" << noise << ", " << amp.str() << "));\n";
+        else o << "        nv = c_scale(" << noise << ", " << amp.str() << ");\n";
+      }
+      if (K.nimp > 0)
+        o << "        if (!vp.origin) { const float rd = 1.0f / (" << imp.str()
+          << "); nv = make_float2(nv.x * rd, nv.y * rd); }\n";
+    }
+    o << "        return nv;\n      }\n";
+  }
+  o << "    }\n    return make_float2(0.f, 0.f);\n  }\n};\n}  // namespace cupssgb\n"
+    << "extern \"C\" __global__ void __launch_bounds__(256, 2) cupssgb_turn(const cupssgb::LineParams P) {\n"
+    << "  cupssgb::turn_body<" << L << ", " << NL << ", cupssgb::GenProg>(P);\n}\n";
+  return o.str();
+}
+
+cudaKernel_t jit_kernel(const std::string& source, const char* entry) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_cache.find(source);
+  if (it != g_cache.end()) return it->second;
+  int dev = 0, major = 0, minor = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+  // sm_103a on GB300; other Blackwell parts get their own arch-specific target
+  const std::string arch = "--gpu-architecture=sm_" + std::to_string(major * 10 + minor) + "a";
+  nvrtcProgram prog;
+  if (nvrtcCreateProgram(&prog, source.c_str(), "cupssgb_turn.cu", kJitNumHeaders, kJitHeaderSources,
+                         kJitHeaderNames) != NVRTC_SUCCESS)
+    throw Error(kErrCuda, "nvrtcCreateProgram failed");
+  const char* opts[] = {arch.c_str(), "--std=c++17", "-lineinfo"};
+  const nvrtcResult rc = nvrtcCompileProgram(prog, 3, opts);
+  if (rc != NVRTC_SUCCESS) {
+    size_t n = 0;
+    nvrtcGetProgramLogSize(prog, &n);
+    std::string log(n, '\0');
+    nvrtcGetProgramLog(prog, &log[0]);
+    nvrtcDestroyProgram(&prog);
+    throw Error(kErrCuda, "NVRTC compilation of the update program failed:\n" + log);
+  }
+  size_t n = 0;
+  nvrtcGetCUBINSize(prog, &n);
+  std::vector<char> cubin(n);
+  nvrtcGetCUBIN(prog, cubin.data());
+  nvrtcDestroyProgram(&prog);
+  cudaLibrary_t lib;
+  cudaError_t e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+  if (e != cudaSuccess) throw Error(kErrCuda, std::string("cudaLibraryLoadData: ") + cudaGetErrorString(e));
+  cudaKernel_t k;
+  e = cudaLibraryGetKernel(&k, lib, entry);
+  if (e != cudaSuccess) throw Error(kErrCuda, std::string("cudaLibraryGetKernel: ") + cudaGetErrorString(e));
+  e = cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+  if (e != cudaSuccess) throw Error(kErrCuda, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+  g_cache[source] = k;
+  return k;
+}
+
+std::string jit_compile_only(const std::string& source, size_t* cubin_bytes) {
+  nvrtcProgram prog;
+  if (nvrtcCreateProgram(&prog, source.c_str(), "cupssgb_turn.cu", kJitNumHeaders, kJitHeaderSources,
+                         kJitHeaderNames) != NVRTC_SUCCESS)
+    return "nvrtcCreateProgram failed";
+  const char* opts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "-lineinfo"};
+  const nvrtcResult rc = nvrtcCompileProgram(prog, 3, opts);
+  size_t n = 0;
+  nvrtcGetProgramLogSize(prog, &n);
+  std::string log(n, '\0');
+  nvrtcGetProgramLog(prog, &log[0]);
+  if (rc == NVRTC_SUCCESS && cubin_bytes) nvrtcGetCUBINSize(prog, cubin_bytes);
+  nvrtcDestroyProgram(&prog);
+  return rc == NVRTC_SUCCESS ? std::string() : log;
+}
+
+}  // namespace cupssgb

@@ -1,33 +1,36 @@
-// Instantiates line_pass<L, 1/2> and its launcher for one line length.
+// Instantiates line_pass<L>, turn_pass<L, 1/2> and the launcher for one line length.
 #pragma once
 #include "kernels.cuh"
 #include "launch.h"
+#include "turn.cuh"
 
-#define CUPSSGB_LINE_INST(L)                                                                   \
-  namespace cupssgb {                                                                          \
-  cudaError_t launch_line_##L(const LineParams& p, int nl, size_t smem, dim3 grid,             \
-                              cudaStream_t st) {                                               \
-    static bool attr1 = false, attr2 = false;                                                  \
-    dim3 block(p.W, LineCfg<L>::M, nl);                                                        \
-    if (nl == 2) {                                                                             \
-      if (!attr2) {                                                                            \
-        cudaError_t e = cudaFuncSetAttribute(line_pass<L, 2>,                                  \
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,     \
-                                             220 * 1024);                                      \
-        if (e != cudaSuccess) return e;                                                        \
-        attr2 = true;                                                                          \
-      }                                                                                        \
-      line_pass<L, 2><<<grid, block, smem, st>>>(p);                                           \
-    } else {                                                                                   \
-      if (!attr1) {                                                                            \
-        cudaError_t e = cudaFuncSetAttribute(line_pass<L, 1>,                                  \
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,     \
-                                             220 * 1024);                                      \
-        if (e != cudaSuccess) return e;                                                        \
-        attr1 = true;                                                                          \
-      }                                                                                        \
-      line_pass<L, 1><<<grid, block, smem, st>>>(p);                                           \
-    }                                                                                          \
-    return cudaGetLastError();                                                                 \
-  }                                                                                            \
+namespace cupssgb {
+template <class K>
+static cudaError_t set_smem_attr(K kernel, bool& done) {
+  if (done) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+  if (e == cudaSuccess) done = true;
+  return e;
+}
+}  // namespace cupssgb
+
+#define CUPSSGB_LINE_INST(L)                                                                    \
+  namespace cupssgb {                                                                           \
+  cudaError_t launch_line_##L(const LineParams& p, int nl, size_t smem, dim3 grid,              \
+                              cudaStream_t st) {                                                \
+    static bool a0 = false, a1 = false, a2 = false;                                             \
+    dim3 block(p.W, LineCfg<L>::M, nl);                                                         \
+    cudaError_t e = cudaSuccess;                                                                \
+    if (p.mode != kModeTurn) {                                                                  \
+      e = set_smem_attr(line_pass<L>, a0);                                                      \
+      if (e == cudaSuccess) line_pass<L><<<grid, block, smem, st>>>(p);                         \
+    } else if (nl == 2) {                                                                       \
+      e = set_smem_attr(turn_pass<L, 2>, a2);                                                   \
+      if (e == cudaSuccess) turn_pass<L, 2><<<grid, block, smem, st>>>(p);                      \
+    } else {                                                                                    \
+      e = set_smem_attr(turn_pass<L, 1>, a1);                                                   \
+      if (e == cudaSuccess) turn_pass<L, 1><<<grid, block, smem, st>>>(p);                      \
+    }                                                                                           \
+    return e != cudaSuccess ? e : cudaGetLastError();                                          \
+  }                                                                                             \
   }

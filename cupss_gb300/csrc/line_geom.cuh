@@ -1,0 +1,63 @@
+// Thread -> (column, line, position) mapping shared by the line passes.
+//
+// A CTA owns W consecutive kx' columns of NL lines of length L along the line axis.
+// Block (W, M, NL): threadIdx.x = column within the tile (fastest, so global
+// accesses of one warp cover contiguous kx'), threadIdx.y = m (FFT thread of the
+// line), threadIdx.z = line of the tile.  Geometries:
+//   kGeoCol : lines along y of a 2D/1D array      elem = y*Lx + kx'
+//   kGeoY3  : lines along y of a 3D array         elem = (z*sy + y)*Lx + kx', blockIdx.y = z
+//   kGeoZ3  : lines along z of a 3D array         elem = (z*sy + ky)*Lx + kx', blockIdx.y = ky,
+//             or, with NL = 2, the pair {p, sy-p} (p >= 1) / {0, sy/2} (p = 0) so that the
+//             Hermitian partner (-ky, -kz) of every point of the packed column kx' = 0 is
+//             in the same CTA.
+// Shared-memory slots hold NL * PL * W float2, position n of line `line` of column w at
+// (line*PL + pad_pos(n))*W + w.
+#pragma once
+#include "engine_types.h"
+#include "fft.cuh"
+
+namespace cupssgb {
+
+template <int L, int NL>
+struct LineGeom {
+  static constexpr int PL = padded_len<L>();
+  int W, w, m, l, kx0, kxp, lineky;
+  bool ok;
+  size_t lbase, pstride, slot_sz;
+  __device__ __forceinline__ explicit LineGeom(const LineParams& P) {
+    W = P.W;
+    w = threadIdx.x;
+    m = threadIdx.y;
+    l = threadIdx.z;
+    kx0 = blockIdx.x * W;
+    kxp = kx0 + w;
+    lineky = 0;
+    bool lineok = true;
+    const int Lx = P.Lx;
+    if (P.geo == kGeoCol) {
+      lbase = kxp;
+      pstride = Lx;
+    } else if (P.geo == kGeoY3) {
+      lbase = (size_t)blockIdx.y * P.sy * Lx + kxp;
+      pstride = Lx;
+    } else {
+      if (NL == 2) {
+        const int pr = blockIdx.y;
+        lineky = (l == 0) ? pr : ((pr == 0) ? P.sy / 2 : P.sy - pr);
+        lineok = !(l == 1 && P.sy == 1);
+      } else {
+        lineky = blockIdx.y;
+      }
+      lbase = (size_t)lineky * Lx + kxp;
+      pstride = (size_t)P.sy * Lx;
+    }
+    ok = (kxp < Lx) && lineok;
+    slot_sz = (size_t)NL * PL * W;
+  }
+  __device__ __forceinline__ size_t elem(int pos) const { return lbase + (size_t)pos * pstride; }
+  __device__ __forceinline__ size_t sidx(int line, int pos) const {
+    return (size_t)(line * PL + pad_pos<L>(pos)) * W + w;
+  }
+};
+
+}  // namespace cupssgb

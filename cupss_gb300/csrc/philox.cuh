@@ -5,8 +5,10 @@
 // (src/field_init.cpp:130-137, src/field.cpp:300-316): the noise is drawn directly in
 // Fourier space inside the update, so it costs no memory traffic.
 #pragma once
+#if !defined(__CUDACC_RTC__)
 #include <cstdint>
 #include <cuda_runtime.h>
+#endif
 
 namespace cupssgb {
 
@@ -29,18 +31,35 @@ __device__ __forceinline__ void philox4x32_10(uint32_t& c0, uint32_t& c1, uint32
   }
 }
 
-// Two standard normals from counter (ctr, step, fid, 0) under key (k0, k1).
-__device__ __forceinline__ void philox_normal2(uint32_t ctr, uint32_t step, uint32_t fid,
-                                               uint32_t k0, uint32_t k1, float& g1, float& g2) {
+// Box-Muller: two standard normals from two 32-bit words.
+//   u1 = ((a >> 8) + 1) 2^-24 in (0, 1],  u2 = (b >> 8) 2^-24 in [0, 1)
+//   r = sqrt(-2 ln u1),  theta = 2 pi (u2 - 1/2) in [-pi, pi)
+__device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float& g1, float& g2) {
+  const float u1 = (float)((a >> 8) + 1u) * 5.9604644775390625e-08f;
+  const float u2 = (float)(b >> 8) * 5.9604644775390625e-08f;
+  const float r = sqrtf(-2.0f * logf(u1));
+  float sn, cs;
+  __sincosf(6.2831853071795864769f * (u2 - 0.5f), &sn, &cs);
+  g1 = r * cs;
+  g2 = r * sn;
+}
+
+// Four standard normals from counter (ctr, step, fid, 0) under key (k0, k1):
+// (g1, g2) from words 0, 1 and (g3, g4) from words 2, 3.
+__device__ __forceinline__ void philox_normal4(uint32_t ctr, uint32_t step, uint32_t fid, uint32_t k0,
+                                               uint32_t k1, float& g1, float& g2, float& g3, float& g4) {
   uint32_t c0 = ctr, c1 = step, c2 = fid, c3 = 0u;
   philox4x32_10(c0, c1, c2, c3, k0, k1);
-  const float u1 = (float)((c0 >> 8) + 1u) * 5.9604644775390625e-08f;   // (0, 1]
-  const float u2 = (float)(c1 >> 8) * 5.9604644775390625e-08f;          // [0, 1)
-  const float r = sqrtf(-2.0f * logf(u1));
-  float s, c;
-  sincospif(2.0f * u2, &s, &c);
-  g1 = r * c;
-  g2 = r * s;
+  box_muller(c0, c1, g1, g2);
+  box_muller(c2, c3, g3, g4);
+}
+
+// Two standard normals from words 0, 1 of counter (ctr, step, fid, 0).
+__device__ __forceinline__ void philox_normal2(uint32_t ctr, uint32_t step, uint32_t fid, uint32_t k0,
+                                               uint32_t k1, float& g1, float& g2) {
+  uint32_t c0 = ctr, c1 = step, c2 = fid, c3 = 0u;
+  philox4x32_10(c0, c1, c2, c3, k0, k1);
+  box_muller(c0, c1, g1, g2);
 }
 #endif
 

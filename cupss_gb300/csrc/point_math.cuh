@@ -1,0 +1,173 @@
+// Per-mode Fourier-space math of the update: q-grid, term multipliers, implicit
+// factors, noise amplitude and Fourier-space noise, dealias mask, packed-column
+// unpacking.  Shared by the interpreted and the generated (NVRTC) update programs.
+#pragma once
+#include "engine_types.h"
+#include "fft.cuh"
+#include "philox.cuh"
+
+namespace cupssgb {
+
+struct VPoint {
+  int kx, ky, kz;
+  bool origin, nyx, nyy, nyz;
+  float qx, qy, qz, q2;
+};
+
+__device__ __forceinline__ float q_of(int k, int n, float step) {
+  return (float)(k < (n + 1) / 2 ? k : k - n) * step;   // src/field_init.cpp:248-250
+}
+
+__device__ __forceinline__ VPoint make_vpoint(const LineParams& P, int kx, int ky, int kz) {
+  VPoint vp;
+  vp.kx = kx;
+  vp.ky = ky;
+  vp.kz = kz;
+  vp.origin = (kx == 0 && ky == 0 && kz == 0);
+  vp.nyx = (P.sx > 1) && (2 * kx == P.sx);
+  vp.nyy = (P.sy > 1) && (2 * ky == P.sy);
+  vp.nyz = (P.sz > 1) && (2 * kz == P.sz);
+  vp.qx = q_of(kx, P.sx, P.stepqx);
+  vp.qy = q_of(ky, P.sy, P.stepqy);
+  vp.qz = q_of(kz, P.sz, P.stepqz);
+  vp.q2 = vp.qx * vp.qx + vp.qy * vp.qy + vp.qz * vp.qz;
+  return vp;
+}
+
+__device__ __forceinline__ float ipow(float x, int n) {
+  float r = 1.f;
+  for (int i = 0; i < n; ++i) r *= x;
+  return r;
+}
+
+// Effective Fourier multiplier of one explicit term.  The reference multiplies the
+// full C2C spectrum by i^s * P(q) (term_init.cpp:135-200) and then projects onto real
+// fields each step (field.cpp:63-89).  On the half spectrum that projection keeps a
+// monomial only when s + sum of its iq exponents over the axes that are NOT at their
+// Nyquist index is even (at a Nyquist index q_a(-k) = q_a(k) under the reference's
+// q convention, so odd powers there do not survive the projection).
+__device__ __forceinline__ float term_mult(const LineParams& P, const TermK& T, const VPoint& vp) {
+  float acc = 0.f;
+  for (int j = 0; j < T.npres; ++j) {
+    const PresK pr = P.pres[T.pres0 + j];
+    const int e = T.s + (vp.nyx ? 0 : pr.iqx) + (vp.nyy ? 0 : pr.iqy) + (vp.nyz ? 0 : pr.iqz);
+    if (e & 1) continue;
+    float v = pr.pre;
+    v *= ipow(vp.q2, pr.q2n);
+    v *= ipow(vp.qx, pr.iqx);
+    v *= ipow(vp.qy, pr.iqy);
+    v *= ipow(vp.qz, pr.iqz);
+    if (pr.invq > 0) {
+      const float iq = vp.origin ? 0.f : 1.0f / sqrtf(vp.q2);
+      v *= ipow(iq, pr.invq);
+    }
+    acc += v;
+  }
+  return acc;
+}
+
+// 1 - dt*sum implicit (dynamic, precalculateImplicit, field_init.cpp:242-267) or
+// sum implicit (non-dynamic, setNotDynamic_k, field_kernels.cu:167-188).
+__device__ __forceinline__ float implicit_factor(const LineParams& P, const FieldK& F, const VPoint& vp) {
+  float acc = F.dynamic ? 1.f : 0.f;
+  for (int j = 0; j < F.nimp; ++j) {
+    const PresK pr = P.pres[F.imp0 + j];
+    float v = pr.pre;
+    if (pr.q2n != 0) v *= ipow(vp.q2, pr.q2n);
+    if (pr.invq != 0) {
+      bool nz = F.dynamic ? (vp.kx > 0 || vp.ky > 0) : !vp.origin;
+      const float iq = nz ? 1.0f / sqrtf(vp.q2) : 0.f;
+      v *= ipow(iq, pr.invq);
+    }
+    if (F.dynamic) acc -= P.dt * v;
+    else acc += v;
+  }
+  return acc;
+}
+
+__device__ __forceinline__ float noise_amp(const FieldK& F, const VPoint& vp) {
+  float a = F.noise_base;
+  if (F.noise_q2n != 0) a *= sqrtf(ipow(vp.q2, F.noise_q2n));
+  if (F.noise_invq != 0) {
+    const float iq = vp.origin ? 0.f : 1.0f / sqrtf(vp.q2);
+    a *= sqrtf(ipow(iq, F.noise_invq));
+  }
+  return a;
+}
+
+// Fourier-space white noise: the DFT of i.i.d. N(0,1) real noise, i.e. a Hermitian
+// complex Gaussian field with Re, Im ~ N(0, N/2) per independent pair and N(0, N) on
+// self-conjugate modes.  Counters (Philox4x32-10 key = seed, counter = (c, step, fid, 0)):
+//  * modes 0 < kx < sx/2 (their partner has kx > sx/2): the line axis coordinate t
+//    (z in 3D, y in 2D; none in 1D) is folded to t mod Lt/2; c = linear index
+//    ((kz*sy + ky)*sx + kx) with t folded; words 0,1 serve t < Lt/2, words 2,3 the
+//    mode at t + Lt/2 -- one generator call for two modes of the same thread;
+//  * modes on the kx = 0 and kx = sx/2 planes: c = the smaller linear index of the
+//    Hermitian pair (k, -k), words 0,1; the other member takes the conjugate.
+__device__ __forceinline__ int line_axis_len(const LineParams& P) {
+  return P.sz > 1 ? P.sz : (P.sy > 1 ? P.sy : 1);
+}
+
+// Both modes (t, t + Lt/2) of a folded pair, t < Lt/2, 0 < kx < sx/2.
+__device__ __forceinline__ void noise_pair(const LineParams& P, int fid, int kx, int ky, int kz, float2& lo,
+                                           float2& hi) {
+  const uint32_t lin = ((uint32_t)kz * P.sy + ky) * P.sx + kx;
+  float g1, g2, g3, g4;
+  philox_normal4(lin, P.step, (uint32_t)fid, P.key0, P.key1, g1, g2, g3, g4);
+  lo = make_float2(P.sqrtHalfN * g1, P.sqrtHalfN * g2);
+  hi = make_float2(P.sqrtHalfN * g3, P.sqrtHalfN * g4);
+}
+
+// Any mode with kx <= sx/2.
+__device__ __forceinline__ float2 noise_at(const LineParams& P, int fid, int kx, int ky, int kz) {
+  if (kx != 0 && 2 * kx != P.sx) {
+    const int Lt = line_axis_len(P);
+    if (Lt == 1) {
+      float2 lo, hi;
+      noise_pair(P, fid, kx, ky, kz, lo, hi);
+      return lo;
+    }
+    const int h = Lt / 2;
+    int& t = (P.sz > 1) ? kz : ky;
+    const bool upper = t >= h;
+    if (upper) t -= h;
+    float2 lo, hi;
+    noise_pair(P, fid, kx, ky, kz, lo, hi);
+    return upper ? hi : lo;
+  }
+  const uint32_t lin = ((uint32_t)kz * P.sy + ky) * P.sx + kx;
+  const int pky = (P.sy - ky) & (P.sy - 1);
+  const int pkz = (P.sz - kz) & (P.sz - 1);
+  const uint32_t plin = ((uint32_t)pkz * P.sy + pky) * P.sx + kx;
+  uint32_t ctr = lin;
+  bool conj = false;
+  float g1, g2;
+  if (plin < lin) {
+    ctr = plin;
+    conj = true;
+  }
+  philox_normal2(ctr, P.step, (uint32_t)fid, P.key0, P.key1, g1, g2);
+  if (plin == lin) return make_float2(P.sqrtN * g1, 0.f);
+  return make_float2(P.sqrtHalfN * g1, conj ? -P.sqrtHalfN * g2 : P.sqrtHalfN * g2);
+}
+
+// dealias_k mask (src/field_kernels.cu:229-256): keep a mode iff |n| <= N/(order+1)
+// on every axis, n = k or k - N for k > N/2.  The three limits are per-field
+// constants (FieldK::chan_xlimit / chan_ylimit / chan_zlimit).
+__device__ __forceinline__ bool keep_axis(int k, int n, int lim) {
+  const int nk = (k > (n >> 1)) ? n - k : k;
+  return nk <= lim;
+}
+__device__ __forceinline__ bool keep_point(const LineParams& P, const VPoint& vp, const FieldK& F) {
+  return keep_axis(vp.kx, P.sx, F.chan_xlimit) && keep_axis(vp.ky, P.sy, F.chan_ylimit) &&
+         keep_axis(vp.kz, P.sz, F.chan_zlimit);
+}
+
+// Unpacks component `which` (0: kx = 0 plane, 1: kx = sx/2 plane) of a packed value.
+__device__ __forceinline__ float2 unpack(float2 z, float2 zp, int which) {
+  const float2 zc = c_conj(zp);
+  if (which == 0) return c_scale(c_add(z, zc), 0.5f);
+  return c_scale(c_mulmi(c_sub(z, zc)), 0.5f);
+}
+
+}  // namespace cupssgb

@@ -112,6 +112,31 @@ long long cupssgb_solver_launch_count(const cupssgb_solver* s);
 long long cupssgb_solver_device_bytes(const cupssgb_solver* s);
 /* The solver's CUDA stream (cudaStream_t), for callers that order their own work. */
 void* cupssgb_solver_stream(const cupssgb_solver* s);
+/* advance(nsteps) bracketed by CUDA events on the solver's stream; *ms = elapsed. */
+int cupssgb_solver_time_advance(cupssgb_solver* s, int nsteps, double* ms);
+/* Per-kernel timing of subsequent advance calls (events around every launch). */
+int cupssgb_solver_set_kernel_timing(cupssgb_solver* s, int on);
+/* JSON {"kind": {"launches": n, "ms": total}} of the launches timed so far; returns
+ * the full length, writes at most buflen-1 chars plus a NUL. */
+int cupssgb_solver_kernel_report(cupssgb_solver* s, char* buf, int buflen);
+
+/* The update program of each non-empty phase is compiled for the system at prepare
+ * time (NVRTC): straight-line code for its terms and prefactor exponents, numerical
+ * values read from the parameter block.  index selects the phase program (0 = the
+ * first non-empty phase).  Returns the length of the CUDA source; works without a
+ * GPU.  set_generated_programs(0) switches to the table-driven update kernel. */
+int cupssgb_solver_generated_source(cupssgb_solver* s, int index, char* buf, int buflen);
+int cupssgb_solver_set_generated_programs(cupssgb_solver* s, int on);
+/* Compiles a generated source for sm_103a without loading it (no GPU needed).
+ * Returns the cubin size (> 0) or CUPSSGB_ERR_CUDA with the NVRTC log in `log`. */
+int cupssgb_jit_check(const char* source, char* log, int loglen);
+
+/* ---------------- process helpers ---------------- */
+/* Page-locked host memory for the host-buffer entry points (cudaMallocHost). */
+int cupssgb_host_alloc(long long bytes, void** out);
+int cupssgb_host_free(void* p);
+/* Selects the CUDA device of the calling thread for subsequently created solvers. */
+int cupssgb_set_device(int device);
 
 /* ---------------- evolver level ---------------- */
 

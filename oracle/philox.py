@@ -14,15 +14,18 @@ numbers: as easy as 1, 2, 3", SC'11) and the Box-Muller transform.  This module
 restates the same definition in numpy so tests can feed the oracle the exact
 realisation the GPU used:
 
-  key     = (seed mod 2^32, seed >> 32)
-  counter = (lin, step, field_id, 0)       lin = (kz*sy + ky)*sx + kx  (canonical member)
-  u1 = ((x0 >> 8) + 1) * 2^-24 in (0,1],  u2 = (x1 >> 8) * 2^-24 in [0,1)
-  g1 + i g2 = sqrt(-2 ln u1) * exp(2 pi i u2)
-  value at canonical k = sqrt(N/2) (g1 + i g2); at -k the conjugate;
-  self-conjugate k: sqrt(N) g1.
-  Canonical member of a pair: for 0 < kx < sx/2 the point itself (its partner
-  has kx > sx/2); on the kx = 0 and kx = sx/2 planes the member with the
-  smaller linear index.
+  key      = (seed mod 2^32, seed >> 32),  counter = (c, step, field_id, 0)
+  normals  = Box-Muller on a pair of words (a, b):
+             u1 = ((a >> 8) + 1) 2^-24 in (0,1],  u2 = (b >> 8) 2^-24 in [0,1),
+             g1 + i g2 = sqrt(-2 ln u1) exp(2 pi i (u2 - 1/2))
+  modes 0 < kx < sx/2: the line-axis coordinate t (z in 3D, y in 2D, none in 1D)
+             is folded to t mod Lt/2; c = (kz*sy + ky)*sx + kx with t folded; words
+             (0,1) give the mode with t < Lt/2, words (2,3) the mode at t + Lt/2;
+             value sqrt(N/2) (g1 + i g2);
+  modes on the kx = 0 and kx = sx/2 planes: c = smaller linear index of the pair
+             (k, -k), words (0,1); value sqrt(N/2)(g1 + i g2) at that member, the
+             conjugate at the other; self-conjugate modes sqrt(N) g1;
+  modes kx > sx/2: conjugate of the partner (sx - kx, -ky, -kz).
 """
 from __future__ import annotations
 
@@ -61,7 +64,7 @@ def normal_pair(x0, x1, dtype=np.float64):
     u1 = (((x0 >> np.uint32(8)).astype(np.float64) + 1.0) * 2.0 ** -24).astype(dtype)
     u2 = ((x1 >> np.uint32(8)).astype(np.float64) * 2.0 ** -24).astype(dtype)
     r = np.sqrt(-2.0 * np.log(u1))
-    ang = 2.0 * np.pi * u2
+    ang = 2.0 * np.pi * (u2 - 0.5)
     return r * np.cos(ang), r * np.sin(ang)
 
 
@@ -71,21 +74,43 @@ def fourier_noise(sx, sy, sz, seed, step, field_id, dtype=np.complex128):
     k0 = np.uint32(seed & 0xFFFFFFFF)
     k1 = np.uint32((seed >> 32) & 0xFFFFFFFF)
     kz, ky, kx = np.meshgrid(np.arange(sz), np.arange(sy), np.arange(sx), indexing="ij")
-    pkz = (-kz) % sz
-    pky = (-ky) % sy
-    pkx = (-kx) % sx
-    lin = (kz * sy + ky) * sx + kx
-    plin = (pkz * sy + pky) * sx + pkx
-    edge = (kx == 0) | (2 * kx == sx)
-    self_is_canon = np.where(edge, lin <= plin, 2 * kx < sx)
-    canon = np.where(self_is_canon, lin, plin).astype(np.uint32)
-    x0, x1, _, _ = philox4x32_10(canon, np.uint32(step), np.uint32(field_id), np.uint32(0), k0, k1)
-    g1, g2 = normal_pair(x0, x1)
+    out = np.zeros((sz, sy, sx), np.complex128)
     half = np.sqrt(N / 2.0)
-    val = half * (g1 + 1j * g2)
-    val = np.where(self_is_canon, val, np.conj(val))
-    val = np.where(lin == plin, np.sqrt(float(N)) * g1 + 0j, val)
-    return val.astype(dtype)
+    # modes 0 < kx < sx/2: folded line-axis counters, words (0,1) lower / (2,3) upper half
+    Lt = sz if sz > 1 else (sy if sy > 1 else 1)
+    sel = (kx > 0) & (2 * kx < sx)
+    t = kz if sz > 1 else ky
+    if Lt > 1:
+        h = Lt // 2
+        upper = t >= h
+        tf = t - upper * h
+    else:
+        upper = np.zeros_like(t, bool)
+        tf = t
+    fkz = tf if sz > 1 else kz
+    fky = ky if sz > 1 else tf
+    lin_f = ((fkz * sy + fky) * sx + kx).astype(np.uint32)
+    x0, x1, x2, x3 = philox4x32_10(lin_f, np.uint32(step), np.uint32(field_id), np.uint32(0), k0, k1)
+    a1, a2 = normal_pair(x0, x1)
+    b1, b2 = normal_pair(x2, x3)
+    v = np.where(upper, b1 + 1j * b2, a1 + 1j * a2) * half
+    out = np.where(sel, v, out)
+    # kx = 0 and kx = sx/2 planes: canonical member of the Hermitian pair, words (0,1)
+    edge = (kx == 0) | (2 * kx == sx)
+    lin = (kz * sy + ky) * sx + kx
+    plin = ((((-kz) % sz) * sy + ((-ky) % sy)) * sx + kx)
+    canon = np.minimum(lin, plin).astype(np.uint32)
+    y0, y1, _, _ = philox4x32_10(canon, np.uint32(step), np.uint32(field_id), np.uint32(0), k0, k1)
+    c1, c2 = normal_pair(y0, y1)
+    ev = half * (c1 + 1j * c2)
+    ev = np.where(lin > plin, np.conj(ev), ev)
+    ev = np.where(lin == plin, np.sqrt(float(N)) * c1 + 0j, ev)
+    out = np.where(edge, ev, out)
+    # kx > sx/2: conjugate of the partner (sx - kx, -ky, -kz)
+    upper_x = 2 * kx > sx
+    partner = np.conj(out[(-kz) % sz, (-ky) % sy, (-kx) % sx])
+    out = np.where(upper_x, partner, out)
+    return out.astype(dtype)
 
 
 class NoiseProvider:

@@ -1,0 +1,41 @@
+"""The update programs the engine generates for a system compile for sm_103a.
+
+Runs on the CPU: code generation and NVRTC compilation need no GPU.  Every system
+of the parser corpus is lowered through the library's parser (evolver level),
+rebuilt at the solver level and its per-phase programs compiled, for 1D, 2D and
+3D grids (line lengths 1, 16/32, 8)."""
+import pytest
+
+from tests.test_parser_parity import CORPUS
+
+
+def solver_from_ir(ir, shape):
+    import cupss_gb300 as c
+    s = c.Solver(*shape, dt=0.01)
+    names = [f["name"] for f in ir]
+    for f in ir:
+        s.add_field(f["dynamic"])
+    for i, f in enumerate(ir):
+        s.set_implicit(i, f["implicit"])
+        for t in f["terms"]:
+            s.add_term(i, [names.index(n) for n in t["product"]], t["pres"])
+        if f["noisy"]:
+            s.set_noise(i, f["noise"])
+    return s
+
+
+@pytest.mark.parametrize("shape", [(16, 1, 1), (32, 16, 1), (8, 4, 8)])
+@pytest.mark.parametrize("case", range(len(CORPUS)))
+def test_generated_programs_compile(built_lib, case, shape):
+    import cupss_gb300 as c
+    from cupss_gb300.api import jit_check
+    from tests.test_parser_parity import build_lib
+    ir = build_lib(*CORPUS[case])
+    s = solver_from_ir(ir, shape)
+    srcs = s.generated_sources()
+    dyn = any(f["dynamic"] for f in ir)
+    nd = any(not f["dynamic"] for f in ir)
+    assert len(srcs) == int(dyn) + int(nd)
+    for src in srcs:
+        assert "cupssgb_turn" in src
+        assert jit_check(src) > 0

@@ -308,3 +308,29 @@ def test_fft_sizes_round_trip_and_one_step(shape):
             ["dt phi + q^2*(a + k*q^2)*phi = -b*q^2*phi^3 + iqx*iqy*phi^2"], [("phi", "0.001*q^2")])
     r, e, _ = run_case(spec, shape, 0.01, 3, {"phi": init}, seed=6)
     assert rel_l2(e.getReal("phi"), r.real_field("phi")) < 3e-6
+
+
+@pytest.mark.parametrize("which", ["modelh2d", "ch3d"])
+def test_generated_program_matches_table_driven(which, monkeypatch):
+    """The update program compiled for the system (default) and the table-driven
+    update kernel (CUPSSGB_JIT=0) give the same fields."""
+    if which == "modelh2d":
+        shape = (32, 32, 1)
+        spec = ([("phi", 1), ("iqxphi", 0), ("iqyphi", 0), ("lapphi", 0), ("vx", 0), ("vy", 0)],
+                {"a": -1.0, "b": 1.0, "k": 4.0, "eta": 1.0, "T": 0.001},
+                ["dt phi + q^2*(a + k*q^2)*phi = -b*q^2*phi^3 - vx*iqxphi - vy*iqyphi",
+                 "iqxphi = iqx*phi", "iqyphi = iqy*phi", "lapphi = -q^2*phi",
+                 "vx*eta*q^2 = -k*iqxphi*lapphi - k*iqx^2*1/q^2*iqxphi*lapphi - k*iqx*iqy*1/q^2*iqyphi*lapphi",
+                 "vy*eta*q^2 = -k*iqyphi*lapphi - k*iqy^2*1/q^2*iqyphi*lapphi - k*iqx*iqy*1/q^2*iqxphi*lapphi"],
+                [("phi", "2*T")])
+    else:
+        shape = (32, 16, 32)
+        spec = ([("phi", 1)], {"a": -1.0, "b": 1.0, "k": 1.0, "T": 0.01},
+                ["dt phi + q^2*(a + k*q^2)*phi = -b*q^2*phi^3"], [("phi", "2*T*q^2")])
+    init = {spec[0][0][0]: init_field(shape, -0.5, 0.5)}
+    monkeypatch.setenv("CUPSSGB_JIT", "0")
+    _, e0, names = run_case(spec, shape, 0.01, 20, init, seed=4)
+    monkeypatch.setenv("CUPSSGB_JIT", "1")
+    _, e1, _ = run_case(spec, shape, 0.01, 20, init, seed=4)
+    for n in names:
+        assert rel_l2(e1.getReal(n), e0.getReal(n)) < 5e-6, n

@@ -75,6 +75,7 @@ SIGNATURES = {
     "cupssgb_solver_generated_source": (_I, [_P, _I, C.c_char_p, _I]),
     "cupssgb_solver_set_generated_programs": (_I, [_P, _I]),
     "cupssgb_jit_check": (_I, [C.c_char_p, C.c_char_p, _I]),
+    "cupssgb_real_to_fourier_noalloc": (_I, [_P, _P, _I, _I, _I, _P]),
     "cupssgb_host_alloc": (_I, [_LL, C.POINTER(_P)]),
     "cupssgb_host_free": (_I, [_P]),
     "cupssgb_set_device": (_I, [_I]),

@@ -75,6 +75,11 @@ field* find_field(evolver* e, const char* name) {
 }
 }  // namespace
 
+namespace cupssgb {
+// Lets other translation units report through cupssgb_last_error().
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace cupssgb
+
 extern "C" {
 
 const char* cupssgb_last_error(void) { return g_last_error.c_str(); }

@@ -138,6 +138,26 @@ int cupssgb_host_free(void* p);
 /* Selects the CUDA device of the calling thread for subsequently created solvers. */
 int cupssgb_set_device(int device);
 
+/* Forward transform of one real field without any device allocation.  No counterpart
+ * in the reference: it exists for callers that must not let a library allocate
+ * device memory -- e.g. a host application that hands out all GPU memory from its own
+ * fixed arena, where an allocation behind its back breaks its accounting or fails.
+ * real_dev: sx*sy*sz floats on the device; fourier_dev: 2*sx*sy*sz floats on the
+ * device, written with the unnormalised forward transform in the reference's full
+ * complex layout (the same values cupssgb_solver_set_real + cupssgb_solver_get_fourier
+ * give).  Both 8-byte aligned.  stream: a cudaStream_t (NULL = legacy default stream).
+ * Working memory is a fixed device array inside the library (8 MiB of spectrum plus a
+ * 32 KiB twiddle table) that every GPU loading the library holds until the process
+ * exits; fields larger than 2^21 points are rejected with CUPSSGB_ERR_LIMIT.  The
+ * first call on a device also looks up that array's device address and fills the
+ * twiddle table with a synchronous copy, so make that first call before any stream
+ * capture.  All calls share the one array: calls that can run at the same time on the
+ * GPU (different streams, threads or processes sharing a context) race and must be
+ * serialised by the caller.  Nothing in the array has to be cleared between calls:
+ * each call writes every element it later reads. */
+int cupssgb_real_to_fourier_noalloc(const float* real_dev, float* fourier_dev, int sx, int sy, int sz,
+                                    void* stream);
+
 /* ---------------- evolver level ---------------- */
 
 /* evolver(bool with_cuda, sx[, sy[, sz]], dx[, dy[, dz]], dt, writeEvery)

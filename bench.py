@@ -207,6 +207,70 @@ def run_cpu_baseline(wl, steps_budget_s=20.0, max_steps=None, workers=None):
                           n, shape[0], shape[1], shape[2], workers, el)}
 
 
+def cufft_reference_schedule(wl, steps, warmup):
+    """The reference GPU step restated op for op with cuFFT (torch.fft) on this GPU.
+
+    Per time step of a dynamic field with one product term and noise, the reference
+    runs (src/field.cpp:15-92, src/term.cpp:12-25): real N(0,1) noise + C2C FFT, the
+    product of the dealiased real field, its C2C FFT, the prefactor multiply, the
+    semi-implicit update, the dealias mask, two inverse C2C FFTs, two normalisations
+    and two forward C2C FFTs.  Tables (prefactor, implicit, noise amplitude) are
+    precomputed like the reference does.  Timed with CUDA events on torch's stream."""
+    import torch
+    sx, sy, sz = wl["shape"]
+    dev = torch.device("cuda")
+    N = sx * sy * sz
+    pi = 3.1415926535
+    def qax(n):
+        i = torch.arange(n, device=dev)
+        return torch.where(i < (n + 1) // 2, i, i - n).float() * (2 * pi / n)
+    qz, qy, qx = torch.meshgrid(qax(sz), qax(sy), qax(sx), indexing="ij")
+    q2 = qx * qx + qy * qy + qz * qz
+    a, b, k, T = (wl["params"][n] for n in ("a", "b", "k", "T"))
+    dt = wl["dt"]
+    pre = (-b * q2).float()                                  # term prefactor table
+    imp = (1.0 + dt * (a * q2 + k * q2 * q2)).float()        # 1 - dt * sum implicit
+    amp = (torch.sqrt(torch.tensor(dt * 2 * T)) * torch.sqrt(q2)).float() if wl["noise"] else None
+    def nk(i, n):
+        return torch.where(i > n // 2, i - n, i).abs()
+    kz, ky, kx = torch.meshgrid(torch.arange(sz, device=dev), torch.arange(sy, device=dev),
+                                torch.arange(sx, device=dev), indexing="ij")
+    mask = ((nk(kx, sx) <= sx // 4) & (nk(ky, sy) <= sy // 4) & (nk(kz, sz) <= sz // 4)).float()
+    from cupss_gb300.workloads import splitmix64_uniform
+    real = torch.from_numpy(splitmix64_uniform(N, 20261203, *wl["init"]).reshape(sz, sy, sx)).to(dev)
+    comp = torch.fft.fftn(real.to(torch.complex64))
+    real_d = torch.zeros_like(real)
+    inv_n = 1.0 / N
+
+    def step():
+        nonlocal comp, real_d
+        noise = torch.fft.fftn(torch.randn(sz, sy, sx, device=dev).to(torch.complex64)) if amp is not None else None
+        term = torch.fft.fftn((real_d * real_d * real_d).to(torch.complex64)) * pre
+        c = comp + dt * term
+        if noise is not None:
+            c = c + amp * noise
+        c = c / imp
+        cd = c * mask
+        r = torch.fft.ifftn(c, norm="forward").real * inv_n
+        real_d = torch.fft.ifftn(cd, norm="forward").real * inv_n
+        comp = torch.fft.fftn(r.to(torch.complex64))
+        torch.fft.fftn(real_d.to(torch.complex64))           # the reference's unused dealiased FFT
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    return {"ms_per_step": ms, "value": N / (ms * 1e-3), "unit": "pt-steps/s", "steps": steps,
+            "what": "reference GPU step sequence restated with cuFFT C2C via torch.fft (6 FFTs + "
+                    "elementwise passes per step, no device syncs), same workload and GPU"}
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -241,6 +305,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--profile-steps", type=int, default=100)
+    ap.add_argument("--no-cufft-ref", action="store_true")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     K = args.steps if args.steps is not None else wl["steps"]
@@ -360,6 +425,13 @@ def main():
                              "finite": bool(np.isfinite(out).all())}
         e2.close()
 
+    cufft_ref = None
+    if not args.no_cufft_ref and wl["shape"][2] > 1:
+        try:
+            cufft_ref = cufft_reference_schedule(wl, steps=50, warmup=5)
+        except Exception as ex:   # torch missing or out of memory: report why
+            cufft_ref = {"unavailable": repr(ex)[:200]}
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         cpu = run_cpu_baseline(wl)
@@ -369,7 +441,8 @@ def main():
                 "warmup": W, "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic: SplitMix64 seed 20261203 uniform initial "
                 "field, Fourier-space Philox noise seed 42", "config": cfg, "roofline": roof,
-                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk}
+                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+                "cufft_reference_schedule": cufft_ref}
         print(json.dumps(line), flush=True)
     e.close()
     if ws > 1:

@@ -242,6 +242,14 @@ class Evolver:
     def getCurrentTimestep(self):
         return self.lib.cupssgb_evolver_current_step(self.h)
 
+    def setCallback(self, name, fn, fourier=False):
+        """fn(evolver_ptr, field_ptr, sx, sy, sz) -> None, or None to remove.  The ctypes
+        wrapper is kept alive by this object."""
+        cb = capi.CALLBACK(fn) if fn is not None else capi.CALLBACK()
+        self._callbacks = getattr(self, "_callbacks", {})
+        self._callbacks[(name, bool(fourier))] = cb
+        return capi.check(self.lib.cupssgb_evolver_set_callback(self.h, name.encode(), int(bool(fourier)), cb))
+
     def describe(self):
         n = self.lib.cupssgb_evolver_describe(self.h, None, 0)
         buf = C.create_string_buffer(n + 1)

@@ -43,6 +43,9 @@ _S = C.c_char_p
 _LL = C.c_longlong
 _ULL = C.c_ulonglong
 
+# cupssgb_callback: void (*)(void* evolver, float* field_pairs, int sx, int sy, int sz)
+CALLBACK = C.CFUNCTYPE(None, _P, _P, _I, _I, _I)
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "cupssgb_last_error": (_S, []),
@@ -65,6 +68,11 @@ SIGNATURES = {
     "cupssgb_solver_get_fourier": (_I, [_P, _I, _FP]),
     "cupssgb_solver_get_fourier_device": (_I, [_P, _I, _P]),
     "cupssgb_solver_synchronize": (_I, [_P]),
+    "cupssgb_solver_advance_phase": (_I, [_P, _I]),
+    "cupssgb_solver_get_real_pairs_device": (_I, [_P, _I, _P]),
+    "cupssgb_solver_get_dealiased_pairs_device": (_I, [_P, _I, _P]),
+    "cupssgb_solver_set_fourier_device": (_I, [_P, _I, _P]),
+    "cupssgb_solver_set_real_pairs_device": (_I, [_P, _I, _P, _P]),
     "cupssgb_solver_step_count": (_LL, [_P]),
     "cupssgb_solver_launch_count": (_LL, [_P]),
     "cupssgb_solver_device_bytes": (_LL, [_P]),
@@ -98,6 +106,7 @@ SIGNATURES = {
     "cupssgb_evolver_current_step": (_I, [_P]),
     "cupssgb_evolver_describe": (_I, [_P, C.c_char_p, _I]),
     "cupssgb_evolver_solver": (_P, [_P]),
+    "cupssgb_evolver_set_callback": (_I, [_P, _S, _I, CALLBACK]),
 }
 
 _lib = None

@@ -229,6 +229,52 @@ int cupssgb_solver_get_fourier_device(cupssgb_solver* s, int field, float* dev_c
   });
 }
 
+int cupssgb_solver_advance_phase(cupssgb_solver* s, int phase) {
+  NEED(s);
+  return guard([&] {
+    s->s->advance_phase(phase);
+    return 0;
+  });
+}
+
+int cupssgb_solver_get_real_pairs_device(cupssgb_solver* s, int field, float* dev_pairs) {
+  NEED(s);
+  NEED(dev_pairs);
+  return guard([&] {
+    s->s->get_real_pairs_device(field, reinterpret_cast<float2*>(dev_pairs));
+    return 0;
+  });
+}
+
+int cupssgb_solver_get_dealiased_pairs_device(cupssgb_solver* s, int field, float* dev_pairs) {
+  NEED(s);
+  NEED(dev_pairs);
+  return guard([&] {
+    s->s->get_dealiased_pairs_device(field, reinterpret_cast<float2*>(dev_pairs));
+    return 0;
+  });
+}
+
+int cupssgb_solver_set_fourier_device(cupssgb_solver* s, int field, const float* dev_complex) {
+  NEED(s);
+  NEED(dev_complex);
+  return guard([&] {
+    s->s->set_fourier_device(field, reinterpret_cast<const float2*>(dev_complex));
+    return 0;
+  });
+}
+
+int cupssgb_solver_set_real_pairs_device(cupssgb_solver* s, int field, const float* dev_pairs,
+                                         const float* dev_dealiased_pairs) {
+  NEED(s);
+  NEED(dev_pairs);
+  return guard([&] {
+    s->s->set_real_pairs_device(field, reinterpret_cast<const float2*>(dev_pairs),
+                                reinterpret_cast<const float2*>(dev_dealiased_pairs));
+    return 0;
+  });
+}
+
 int cupssgb_solver_synchronize(cupssgb_solver* s) {
   NEED(s);
   return guard([&] {
@@ -530,5 +576,22 @@ int cupssgb_evolver_describe(const cupssgb_evolver* ce, char* buf, int buflen) {
 }
 
 cupssgb_solver* cupssgb_evolver_solver(cupssgb_evolver* e) { return e ? e->e->solverHandle() : nullptr; }
+
+int cupssgb_evolver_set_callback(cupssgb_evolver* e, const char* name, int fourier, cupssgb_callback fn) {
+  NEED(e);
+  return guard([&] {
+    field* f = find_field(e->e, name);
+    if (!f) return fail(CUPSSGB_ERR_INVALID, std::string("no field ") + (name ? name : ""));
+    auto cb = reinterpret_cast<void (*)(evolver*, float2*, int, int, int)>(fn);
+    if (fourier) {
+      f->hasCBFourier = fn != nullptr;
+      f->callbackFourier = cb;
+    } else {
+      f->hasCB = fn != nullptr;
+      f->callback = cb;
+    }
+    return 0;
+  });
+}
 
 }  // extern "C"

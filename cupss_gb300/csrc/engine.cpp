@@ -29,6 +29,9 @@ Solver::Solver(int sx, int sy, int sz, float dx, float dy, float dz, float dt)
     : sx_(sx), sy_(sy), sz_(sz), dx_(dx), dy_(dy), dz_(dz), dt_(dt) {
   const char* jit = std::getenv("CUPSSGB_JIT");
   use_jit_ = !(jit && std::string(jit) == "0");
+  // turnaround launch shape: tile width and resident CTAs per SM (tuning knobs)
+  if (const char* w = std::getenv("CUPSSGB_TURN_W")) turn_w_ = std::atoi(w);
+  if (const char* b = std::getenv("CUPSSGB_TURN_MINB")) turn_min_blocks_ = std::max(1, std::atoi(b));
   if (!pow2(sx) || sx < 2 || sx > 2048 || !pow2(sy) || sy > 1024 || !pow2(sz) || sz > 1024)
     throw Error(kErrUnsupported,
                 "grid sizes must be powers of two: 2 <= sx <= 2048, 1 <= sy, sz <= 1024");
@@ -331,14 +334,120 @@ void Solver::get_real(int f, float* dst, bool on_device) {
   if (!on_device) check(cudaStreamSynchronize(stream_), "get_real sync");
 }
 
+void Solver::row_pass_simple(int in_mode, const void* in, int out_mode, void* out, float scale) {
+  XParams x;
+  std::memset(&x, 0, sizeof(x));
+  x.Lx = Lx_;
+  x.rows = sy_ * sz_;
+  x.in_mode = in_mode;
+  x.out_mode = out_mode;
+  x.out_scale = scale;
+  x.n_in = 1;
+  x.in[0] = reinterpret_cast<const float2*>(in);
+  x.n_prod = 1;
+  x.out[0] = out;
+  x.prod_n[0] = 1;
+  x.prod_f[0][0] = 0;
+  x.tw = tw_;
+  check(launch_row_pass(x, stream_), "row pass");
+  ++launches_;
+}
+
+void Solver::forward_lines(float2* st) {
+  if (dim_ == 3) {
+    line_fwd_inv(kGeoY3, kModeFwd, st, st, Lx_);
+    line_fwd_inv(kGeoZ3, kModeFwd, st, st, Lx_);
+  } else if (sy_ > 1) {
+    line_fwd_inv(kGeoCol, kModeFwd, st, st, Lx_);
+  }
+}
+
 void Solver::get_real_pairs_device(int f, float2* dst) {
   if (!prepared_) throw Error(kErrState, "get_real before prepare");
-  to_real_scratch(f);
-  // widen into the reference's float2 (x, 0) layout with a copy2D: x <- real, y <- 0
-  check(cudaMemsetAsync(dst, 0, npoints() * sizeof(float2), stream_), "memset pairs");
-  check(cudaMemcpy2DAsync(dst, sizeof(float2), scratch_real_, sizeof(float), sizeof(float), npoints(),
-                          cudaMemcpyDeviceToDevice, stream_),
-        "widen pairs");
+  if (f < 0 || f >= nfields()) throw Error(kErrInvalid, "bad field index");
+  const float2* st = state_[par_[f]][f];
+  const float2* spec = st;
+  if (dim_ == 3) {
+    line_fwd_inv(kGeoZ3, kModeInv, st, scratch_spec_, Lx_);
+    line_fwd_inv(kGeoY3, kModeInv, scratch_spec_, scratch_spec_, Lx_);
+    spec = scratch_spec_;
+  } else if (sy_ > 1) {
+    line_fwd_inv(kGeoCol, kModeInv, st, scratch_spec_, Lx_);
+    spec = scratch_spec_;
+  }
+  row_pass_simple(kXInSpectral, spec, kXOutRealPair, dst, 1.0f / (float)npoints());
+}
+
+void Solver::get_dealiased_pairs_device(int f, float2* dst) {
+  if (!prepared_) throw Error(kErrState, "get_dealiased before prepare");
+  if (f < 0 || f >= nfields() || alias_order_[f] <= 1) throw Error(kErrInvalid, "field has no dealiased copy");
+  // Rebuilt from the state rather than read from the channel: after a real-space
+  // callback the channel holds the callback's full x spectrum, and the turnaround
+  // rewrites only the columns below the dealias limit.
+  channel_from_state(f, scratch_spec_);
+  row_pass_simple(kXInSpectral, scratch_spec_, kXOutRealPair, dst, 1.0f);
+}
+
+void Solver::channel_from_state(int f, float2* dst) {
+  // dst <- inverse y/z lines of (masked state / N): the channel layout (x spectrum,
+  // y and z positional) that the row pass turns into the dealiased real field.
+  MaskParams mp;
+  mp.sx = sx_;
+  mp.sy = sy_;
+  mp.sz = sz_;
+  mp.Lx = Lx_;
+  mp.xlim = sx_ / (alias_order_[f] + 1);
+  mp.ylim = sy_ / (alias_order_[f] + 1);
+  mp.zlim = sz_ / (alias_order_[f] + 1);
+  mp.scale = 1.0f / (float)npoints();
+  mp.spec = state_[par_[f]][f];
+  mp.out = scratch_spec_;
+  check(launch_mask(mp, stream_), "mask spectrum");
+  ++launches_;
+  if (dim_ == 3) {
+    line_fwd_inv(kGeoZ3, kModeInv, scratch_spec_, scratch_spec_, Lx_);
+    line_fwd_inv(kGeoY3, kModeInv, scratch_spec_, dst, Lx_);
+  } else if (sy_ > 1) {
+    line_fwd_inv(kGeoCol, kModeInv, scratch_spec_, dst, Lx_);
+  } else if (dst != scratch_spec_) {
+    check(cudaMemcpyAsync(dst, scratch_spec_, (size_t)Lx_ * sizeof(float2), cudaMemcpyDeviceToDevice, stream_),
+          "channel copy");
+  }
+}
+
+void Solver::set_fourier_device(int f, const float2* full) {
+  if (!prepared_) throw Error(kErrState, "set_fourier before prepare");
+  if (f < 0 || f >= nfields()) throw Error(kErrInvalid, "bad field index");
+  CompressParams cp;
+  cp.sx = sx_;
+  cp.sy = sy_;
+  cp.sz = sz_;
+  cp.Lx = Lx_;
+  cp.full = full;
+  cp.spec = state_[par_[f]][f];
+  check(launch_compress(cp, stream_), "compress spectrum");
+  ++launches_;
+  if (alias_order_[f] > 1) channel_from_state(f, chan_[f]);
+}
+
+void Solver::set_real_pairs_device(int f, const float2* real, const float2* dealiased) {
+  if (!prepared_) throw Error(kErrState, "set_real before prepare");
+  if (f < 0 || f >= nfields()) throw Error(kErrInvalid, "bad field index");
+  float2* st = state_[par_[f]][f];
+  row_pass_simple(kXInRealPair, real, kXOutSpectral, st, 1.0f);
+  forward_lines(st);
+  if (alias_order_[f] > 1) {
+    // the channel is the x spectrum scaled by 1/sx (see channel_from_state)
+    if (dealiased) row_pass_simple(kXInRealPair, dealiased, kXOutSpectral, chan_[f], 1.0f / (float)sx_);
+    else channel_from_state(f, chan_[f]);
+  }
+}
+
+void Solver::advance_phase(int phase) {
+  if (!prepared_) throw Error(kErrState, "advance before prepare");
+  if (phase < 0 || phase > 1) throw Error(kErrInvalid, "phase is 0 (non-dynamic) or 1 (dynamic)");
+  run_phase(phases_[phase]);
+  if (phase == 1) ++step_;
 }
 
 void Solver::get_fourier(int f, float2* dst, bool on_device) {
@@ -490,9 +599,10 @@ const std::string& Solver::turn_source(Phase& P, const LineParams& p, int L, int
     const PresK& q = p.pres[j];
     sig.insert(sig.end(), {q.q2n, q.iqx, q.iqy, q.iqz, q.invq});
   }
+  sig.push_back(turn_min_blocks_);
   if (sig != P.jit_sig) {
     P.jit_sig = sig;
-    P.jit_src = jit_generate_turn(p, L, nl);
+    P.jit_src = jit_generate_turn(p, L, nl, turn_min_blocks_);
   }
   return P.jit_src;
 }
@@ -557,6 +667,7 @@ void Solver::run_phase(Phase& P) {
   bool any_chan = false;
   fill_turn(P, p, nslots, any_chan);
   p.W = pick_w(L, nl, nslots);
+  if (turn_w_ > 0 && turn_w_ < p.W) p.W = turn_w_;
   dim3 grid((Lx_ + p.W - 1) / p.W, dim_ == 3 ? std::max(sy_ / 2, 1) : 1);
   mark_begin();
   if (use_jit_) {

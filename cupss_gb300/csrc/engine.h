@@ -73,6 +73,12 @@ class Solver {
   void get_real(int f, float* dst, bool dst_on_device);
   void get_fourier(int f, float2* dst, bool dst_on_device);
   void get_real_pairs_device(int f, float2* dst);   // reference float2 layout (x, 0)
+  // Materialisation points for callbacks (src/field.cpp:48-86), all device pointers in
+  // the reference's layouts, ordered on the solver's stream:
+  void advance_phase(int phase);                    // 0: non-dynamic, 1: dynamic (+ step count)
+  void get_dealiased_pairs_device(int f, float2* dst);
+  void set_fourier_device(int f, const float2* full);          // also re-derives the dealiased copy
+  void set_real_pairs_device(int f, const float2* real, const float2* dealiased);
   void synchronize();
   // Kernel timing: when on, every launch of advance() is bracketed by CUDA events on
   // the solver's stream and its duration is accumulated per kernel kind.
@@ -120,6 +126,9 @@ class Solver {
   int pick_w(int L, int nl, int nslots) const;
   void line_fwd_inv(int geo, int mode, const float2* in, float2* out, int xlimit);
   void to_real_scratch(int f);
+  void row_pass_simple(int in_mode, const void* in, int out_mode, void* out, float scale);
+  void forward_lines(float2* st);
+  void channel_from_state(int f, float2* dst);
   void mark_begin();
   void mark_end(const char* kind);
   void flush_timing();
@@ -132,6 +141,8 @@ class Solver {
   std::vector<int> alias_order_;
   bool prepared_ = false;
   bool use_jit_ = true;
+  int turn_w_ = 0;            // 0: automatic tile width
+  int turn_min_blocks_ = 2;   // __launch_bounds__ min blocks of the generated turnaround
   long long step_ = 0;
   long long launches_ = 0;
   size_t dev_bytes_ = 0;

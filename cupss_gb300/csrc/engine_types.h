@@ -90,13 +90,13 @@ struct LineParams {
   const float2* tw;
 };
 
-enum XInMode : int { kXInSpectral = 0, kXInReal = 1 };
+enum XInMode : int { kXInSpectral = 0, kXInReal = 1, kXInRealPair = 2 };   // RealPair: float2 (x, y) reads .x
 enum XOutMode : int { kXOutSpectral = 0, kXOutReal = 1, kXOutRealPair = 2 };
 
 struct XParams {
   int Lx, rows;
   int in_mode, out_mode;
-  float out_scale;
+  float out_scale;                  // multiplies every product, in real or spectral output
   int n_in;
   const float2* in[kMaxXIn];        // spectral channels (float2) or real rows (as pairs)
   int n_prod;
@@ -110,6 +110,23 @@ struct ExpandParams {
   int sx, sy, sz, Lx;
   const float2* spec;   // packed half spectrum, fully transformed
   float2* full;         // reference layout, sx*sy*sz complex
+};
+
+// Reference-layout full spectrum -> packed half spectrum (Hermitian projection, the
+// effect of the reference's IFFT -> real part -> FFT round trip, src/field.cpp:64-89).
+struct CompressParams {
+  int sx, sy, sz, Lx;
+  const float2* full;
+  float2* spec;
+};
+
+// Dealiased, 1/N-scaled copy of a packed spectrum (kept modes only).
+struct MaskParams {
+  int sx, sy, sz, Lx;
+  int xlim, ylim, zlim;
+  float scale;
+  const float2* spec;
+  float2* out;
 };
 
 }  // namespace cupssgb

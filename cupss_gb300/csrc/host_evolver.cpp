@@ -173,9 +173,6 @@ void evolver::prepareProblem() {
       fatal("Can't create data directory, is there a file called data?");
     }
     _parser->writeParamsToFile("data/parameter_list.txt.0");
-    if (has_callbacks())
-      throw std::runtime_error(
-          "real-space / Fourier-space callbacks are not supported by this build");
     if (!solver_) build_solver();
     if (verbose) std::cout << "Uploading initial states to the device." << std::endl;
     const size_t n = (size_t)sx * sy * sz;
@@ -268,13 +265,107 @@ void evolver::sync_host_arrays() {
   for (field* f : fields) f->copyDeviceToHost();
 }
 
+namespace {
+void cuda_or_die(cudaError_t e, bool throw_errors, const char* what) {
+  if (e == cudaSuccess) return;
+  const std::string msg = std::string(what) + ": " + cudaGetErrorString(e);
+  if (throw_errors) throw std::runtime_error(msg);
+  std::cerr << "CUDA Runtime Error" << std::endl << msg << std::endl;
+  std::exit(1);
+}
+}  // namespace
+
+// One time step with user callbacks (src/field.cpp:48-86).  The engine runs the two
+// phases separately; after each phase every field of that phase that has callbacks is
+// materialised in the reference's layouts, handed to the callback (device pointers in
+// GPU mode, host pointers in RUN_CPU mode) and written back.
+void evolver::run_callbacks_step() {
+  const size_t n = (size_t)sx * sy * sz;
+  auto ok = [&](int rc) {
+    if (rc != 0) {
+      if (throw_errors_) throw std::runtime_error(cupssgb_last_error());
+      fatal(std::string("CUDA Runtime Error\n") + cupssgb_last_error());
+    }
+  };
+  for (int phase = 0; phase < 2; ++phase) {
+    ok(cupssgb_solver_advance_phase(solver_, phase));
+    for (size_t i = 0; i < fields.size(); ++i) {
+      field* f = fields[i];
+      if ((int)f->dynamic != phase || !(f->hasCB || f->hasCBFourier)) continue;
+      if (f->hasCBFourier) {
+        if (f->callbackFourier == nullptr) {
+          std::cout << "Wants to apply callback function in Fourier space but pointer to function is NULL"
+                    << std::endl;
+        } else {
+          if (!f->comp_array_d)
+            cuda_or_die(cudaMalloc((void**)&f->comp_array_d, n * sizeof(float2)), throw_errors_, "cudaMalloc");
+          ok(cupssgb_solver_get_fourier_device(solver_, (int)i, reinterpret_cast<float*>(f->comp_array_d)));
+          ok(cupssgb_solver_synchronize(solver_));
+          if (with_cuda) {
+            f->callbackFourier(this, f->comp_array_d, sx, sy, sz);
+          } else {
+            cuda_or_die(cudaMemcpy(f->comp_array, f->comp_array_d, n * sizeof(float2), cudaMemcpyDeviceToHost),
+                        throw_errors_, "cudaMemcpy");
+            f->callbackFourier(this, f->comp_array, sx, sy, sz);
+            cuda_or_die(cudaMemcpy(f->comp_array_d, f->comp_array, n * sizeof(float2), cudaMemcpyHostToDevice),
+                        throw_errors_, "cudaMemcpy");
+          }
+          cuda_or_die(cudaDeviceSynchronize(), throw_errors_, "Fourier callback");
+          ok(cupssgb_solver_set_fourier_device(solver_, (int)i, reinterpret_cast<float*>(f->comp_array_d)));
+        }
+      }
+      if (f->hasCB) {
+        if (f->callback == nullptr) {
+          std::cout << "Wants to apply callback function but pointer to function is NULL" << std::endl;
+          continue;
+        }
+        if (!f->real_array_d)
+          cuda_or_die(cudaMalloc((void**)&f->real_array_d, n * sizeof(float2)), throw_errors_, "cudaMalloc");
+        if (f->needsaliasing && !f->real_dealiased_d)
+          cuda_or_die(cudaMalloc((void**)&f->real_dealiased_d, n * sizeof(float2)), throw_errors_, "cudaMalloc");
+        ok(cupssgb_solver_get_real_pairs_device(solver_, (int)i, reinterpret_cast<float*>(f->real_array_d)));
+        if (f->needsaliasing)
+          ok(cupssgb_solver_get_dealiased_pairs_device(solver_, (int)i,
+                                                       reinterpret_cast<float*>(f->real_dealiased_d)));
+        ok(cupssgb_solver_synchronize(solver_));
+        if (with_cuda) {
+          f->callback(this, f->real_array_d, sx, sy, sz);
+          if (f->needsaliasing) f->callback(this, f->real_dealiased_d, sx, sy, sz);
+        } else {
+          if (f->needsaliasing && !f->real_dealiased) f->real_dealiased = new float2[n];
+          cuda_or_die(cudaMemcpy(f->real_array, f->real_array_d, n * sizeof(float2), cudaMemcpyDeviceToHost),
+                      throw_errors_, "cudaMemcpy");
+          f->callback(this, f->real_array, sx, sy, sz);
+          cuda_or_die(cudaMemcpy(f->real_array_d, f->real_array, n * sizeof(float2), cudaMemcpyHostToDevice),
+                      throw_errors_, "cudaMemcpy");
+          if (f->needsaliasing) {
+            cuda_or_die(cudaMemcpy(f->real_dealiased, f->real_dealiased_d, n * sizeof(float2),
+                                   cudaMemcpyDeviceToHost),
+                        throw_errors_, "cudaMemcpy");
+            f->callback(this, f->real_dealiased, sx, sy, sz);
+            cuda_or_die(cudaMemcpy(f->real_dealiased_d, f->real_dealiased, n * sizeof(float2),
+                                   cudaMemcpyHostToDevice),
+                        throw_errors_, "cudaMemcpy");
+          }
+        }
+        cuda_or_die(cudaDeviceSynchronize(), throw_errors_, "callback");
+        ok(cupssgb_solver_set_real_pairs_device(solver_, (int)i, reinterpret_cast<float*>(f->real_array_d),
+                                                f->needsaliasing ? reinterpret_cast<float*>(f->real_dealiased_d)
+                                                                 : nullptr));
+      }
+    }
+  }
+}
+
 int evolver::advanceTime() {
   if (!solver_) {
     if (throw_errors_) throw std::runtime_error("advanceTime before prepareProblem");
     fatal("ERROR: advanceTime before prepareProblem");
   }
   if (currentTimeStep % writeEveryNSteps == 0) writeOut();
-  if (cupssgb_solver_advance(solver_, 1) != 0) {
+  if (has_callbacks()) {
+    run_callbacks_step();
+  } else if (cupssgb_solver_advance(solver_, 1) != 0) {
     if (throw_errors_) throw std::runtime_error(cupssgb_last_error());
     fatal(std::string("CUDA Runtime Error\n") + cupssgb_last_error());
   }
@@ -295,7 +386,7 @@ int evolver::advanceTimeSteps(int n) {
   }
   bool any_output = false;
   for (field* f : fields) any_output = any_output || f->outputToFile;
-  if (!with_cuda) {
+  if (!with_cuda || has_callbacks()) {
     for (int i = 0; i < n; ++i) advanceTime();
     return 0;
   }

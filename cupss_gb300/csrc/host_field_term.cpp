@@ -21,6 +21,7 @@ void field::common_constructor() {
   }
   real_array_d = nullptr;
   comp_array_d = nullptr;
+  real_dealiased = nullptr;
   real_dealiased_d = nullptr;
   needsaliasing = false;
   aliasing_order = 1;
@@ -59,6 +60,7 @@ field::field(int _sx, int _sy, int _sz, float _dx, float _dy, float _dz)
 field::~field() {
   delete[] real_array;
   delete[] comp_array;
+  delete[] real_dealiased;
   if (real_array_d) cudaFree(real_array_d);
   if (comp_array_d) cudaFree(comp_array_d);
   if (real_dealiased_d) cudaFree(real_dealiased_d);

@@ -52,7 +52,7 @@ std::string keep_expr(int s, const PresK& p, bool* never) {
 
 }  // namespace
 
-std::string jit_generate_turn(const LineParams& p, int L, int NL) {
+std::string jit_generate_turn(const LineParams& p, int L, int NL, int min_blocks) {
   std::ostringstream o;
   o << "#include \"turn.cuh\"\n"
     << "namespace cupssgb {\n"
@@ -133,7 +133,8 @@ std::string jit_generate_turn(const LineParams& p, int L, int NL) {
     o << "        return nv;\n      }\n";
   }
   o << "    }\n    return make_float2(0.f, 0.f);\n  }\n};\n}  // namespace cupssgb\n"
-    << "extern \"C\" __global__ void __launch_bounds__(256, 2) cupssgb_turn(const cupssgb::LineParams P) {\n"
+    << "extern \"C\" __global__ void __launch_bounds__(256, " << min_blocks
+    << ") cupssgb_turn(const cupssgb::LineParams P) {\n"
     << "  cupssgb::turn_body<" << L << ", " << NL << ", cupssgb::GenProg>(P);\n}\n";
   return o.str();
 }

@@ -57,6 +57,72 @@ __global__ void expand_spectrum(const ExpandParams p) {
   }
 }
 
+__global__ void compress_spectrum(const CompressParams p) {
+  const size_t H = (size_t)p.Lx * p.sy * p.sz;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < H;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int kx = (int)(idx % p.Lx);
+    const int ky = (int)((idx / p.Lx) % p.sy);
+    const int kz = (int)(idx / ((size_t)p.Lx * p.sy));
+    const int pky = (p.sy - ky) & (p.sy - 1);
+    const int pkz = (p.sz - kz) & (p.sz - 1);
+    const size_t row = ((size_t)kz * p.sy + ky) * p.sx, prow = ((size_t)pkz * p.sy + pky) * p.sx;
+    float2 out;
+    if (kx > 0) {
+      // (F(k) + conj F(-k)) / 2, -k = (sx - kx, -ky, -kz)
+      out = c_scale(c_add(p.full[row + kx], c_conj(p.full[prow + (p.sx - kx)])), 0.5f);
+    } else {
+      const float2 c0 = c_scale(c_add(p.full[row], c_conj(p.full[prow])), 0.5f);
+      const int nx = p.sx / 2;
+      const float2 cn = c_scale(c_add(p.full[row + nx], c_conj(p.full[prow + nx])), 0.5f);
+      out = c_add(c0, c_muli(cn));
+    }
+    p.spec[idx] = out;
+  }
+}
+
+__global__ void mask_spectrum(const MaskParams p) {
+  const size_t H = (size_t)p.Lx * p.sy * p.sz;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < H;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int kx = (int)(idx % p.Lx);
+    const int ky = (int)((idx / p.Lx) % p.sy);
+    const int kz = (int)(idx / ((size_t)p.Lx * p.sy));
+    auto keep = [&](int k, int n, int lim) { return ((k > (n >> 1)) ? n - k : k) <= lim; };
+    const bool kyz = keep(ky, p.sy, p.ylim) && keep(kz, p.sz, p.zlim);
+    float2 out = make_float2(0.f, 0.f);
+    if (kx > 0) {
+      if (kyz && keep(kx, p.sx, p.xlim)) out = c_scale(p.spec[idx], p.scale);
+    } else {
+      const int pky = (p.sy - ky) & (p.sy - 1);
+      const int pkz = (p.sz - kz) & (p.sz - 1);
+      const float2 z = p.spec[idx];
+      const float2 zp = p.spec[((size_t)pkz * p.sy + pky) * p.Lx];
+      const float2 c0 = unpack(z, zp, 0), cn = unpack(z, zp, 1);
+      const float2 a = kyz ? c_scale(c0, p.scale) : make_float2(0.f, 0.f);
+      const float2 b = (kyz && keep(p.sx / 2, p.sx, p.xlim)) ? c_scale(cn, p.scale) : make_float2(0.f, 0.f);
+      out = c_add(a, c_muli(b));
+    }
+    p.out[idx] = out;
+  }
+}
+
+cudaError_t launch_compress(const CompressParams& p, cudaStream_t st) {
+  const size_t H = (size_t)p.Lx * p.sy * p.sz;
+  int blocks = (int)((H + 255) / 256);
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  compress_spectrum<<<blocks, 256, 0, st>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mask(const MaskParams& p, cudaStream_t st) {
+  const size_t H = (size_t)p.Lx * p.sy * p.sz;
+  int blocks = (int)((H + 255) / 256);
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  mask_spectrum<<<blocks, 256, 0, st>>>(p);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_expand(const ExpandParams& p, cudaStream_t st) {
   const size_t N = (size_t)p.sx * p.sy * p.sz;
   int blocks = (int)((N + 255) / 256);

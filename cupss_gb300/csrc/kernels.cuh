@@ -90,6 +90,17 @@ row_pass(const XParams p) {
       }
       continue;
     }
+    if (p.in_mode == kXInRealPair) {
+      // reference float2 layout: point 2n at (.x of) element 2n, point 2n+1 at 2n+1
+      const float4* in = reinterpret_cast<const float4*>(p.in[c]) + rowoff;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int n = pos_step1<LX>(m, r);
+        const float4 q = live ? in[n] : make_float4(0.f, 0.f, 0.f, 0.f);
+        V[pad_pos<LX>(n)] = make_float2(q.x, q.z);
+      }
+      continue;
+    }
     const float2* in = p.in[c] + rowoff;
 #pragma unroll
     for (int i = 0; i < R; ++i) {
@@ -115,7 +126,7 @@ row_pass(const XParams p) {
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int a = pad_pos<LX>(pos_step1<LX>(m, r));
-      float2 acc = make_float2(1.f, 1.f);
+      float2 acc = make_float2(p.out_scale, p.out_scale);   // output scale folded into the product
       for (int t = 0; t < p.prod_n[q]; ++t) {
         float2 x = slot(p.prod_f[q][t])[a];
         acc.x *= x.x;
@@ -128,7 +139,7 @@ row_pass(const XParams p) {
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           const int n = pos_step1<LX>(m, r);
-          const float2 z = c_scale(v[r], p.out_scale);
+          const float2 z = v[r];
           if (p.out_mode == kXOutReal) {
             reinterpret_cast<float2*>(p.out[q])[rowoff + n] = z;
           } else {
@@ -214,5 +225,7 @@ line_pass(const LineParams P) {
 
 // Packed half spectrum -> reference-layout full complex spectrum.
 __global__ void expand_spectrum(const ExpandParams p);
+__global__ void compress_spectrum(const CompressParams p);
+__global__ void mask_spectrum(const MaskParams p);
 
 }  // namespace cupssgb

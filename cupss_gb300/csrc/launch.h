@@ -16,6 +16,8 @@ size_t line_pass_smem(int L, int nl, int W, int nslots);
 int line_threads(int L, int nl, int W);
 
 cudaError_t launch_expand(const ExpandParams& p, cudaStream_t st);
+cudaError_t launch_compress(const CompressParams& p, cudaStream_t st);
+cudaError_t launch_mask(const MaskParams& p, cudaStream_t st);
 
 // per-L launchers (one translation unit per group of sizes)
 #define CUPSSGB_DECL_LINE(L) \

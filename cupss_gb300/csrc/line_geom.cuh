@@ -24,12 +24,15 @@ struct LineGeom {
   int W, w, m, l, kx0, kxp, lineky;
   bool ok;
   size_t lbase, pstride, slot_sz;
-  __device__ __forceinline__ explicit LineGeom(const LineParams& P) {
+  __device__ __forceinline__ explicit LineGeom(const LineParams& P) { init(P, blockIdx.x, blockIdx.y); }
+  // Explicit tile coordinates (persistent kernels): tx = kx' tile, ty = line index.
+  __device__ __forceinline__ LineGeom(const LineParams& P, int tx, int ty) { init(P, tx, ty); }
+  __device__ __forceinline__ void init(const LineParams& P, int tx, int ty) {
     W = P.W;
     w = threadIdx.x;
     m = threadIdx.y;
     l = threadIdx.z;
-    kx0 = blockIdx.x * W;
+    kx0 = tx * W;
     kxp = kx0 + w;
     lineky = 0;
     bool lineok = true;
@@ -38,15 +41,15 @@ struct LineGeom {
       lbase = kxp;
       pstride = Lx;
     } else if (P.geo == kGeoY3) {
-      lbase = (size_t)blockIdx.y * P.sy * Lx + kxp;
+      lbase = (size_t)ty * P.sy * Lx + kxp;
       pstride = Lx;
     } else {
       if (NL == 2) {
-        const int pr = blockIdx.y;
+        const int pr = ty;
         lineky = (l == 0) ? pr : ((pr == 0) ? P.sy / 2 : P.sy - pr);
         lineok = !(l == 1 && P.sy == 1);
       } else {
-        lineky = blockIdx.y;
+        lineky = ty;
       }
       lbase = (size_t)lineky * Lx + kxp;
       pstride = (size_t)P.sy * Lx;

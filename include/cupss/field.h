@@ -53,6 +53,7 @@ class field {
 
   bool needsaliasing;
   int aliasing_order;
+  float2* real_dealiased;      // host copy handed to callbacks in RUN_CPU mode
   float2* real_dealiased_d;
 
   std::vector<term*> terms;

@@ -104,6 +104,23 @@ int cupssgb_solver_get_real_device(cupssgb_solver* s, int field, float* dev_real
 /* Fourier-space field (field::comp_array, full complex layout, 2*N floats). */
 int cupssgb_solver_get_fourier(cupssgb_solver* s, int field, float* host_complex);
 int cupssgb_solver_get_fourier_device(cupssgb_solver* s, int field, float* dev_complex);
+/* Materialisation points for user callbacks (field::callback / callbackFourier,
+ * src/field.cpp:48-86).  advance_phase runs one half of a time step: phase 0 updates
+ * the non-dynamic fields, phase 1 the dynamic ones and counts the step (advance(1) ==
+ * phase 0 + phase 1).  Between phases a caller can read a field in the reference's
+ * device layouts, modify it and write it back:
+ *   get_real_pairs_device      real field as N float2 (x, 0)          (real_array_d)
+ *   get_dealiased_pairs_device dealiased real field as N float2 (x, 0) (real_dealiased_d)
+ *   set_fourier_device         full complex spectrum, 2N floats       (comp_array_d);
+ *                              projected onto real fields, dealiased copy re-derived
+ *   set_real_pairs_device      real field (+ optional dealiased copy, NULL = re-derive)
+ * All are ordered on the solver's stream. */
+int cupssgb_solver_advance_phase(cupssgb_solver* s, int phase);
+int cupssgb_solver_get_real_pairs_device(cupssgb_solver* s, int field, float* dev_pairs);
+int cupssgb_solver_get_dealiased_pairs_device(cupssgb_solver* s, int field, float* dev_pairs);
+int cupssgb_solver_set_fourier_device(cupssgb_solver* s, int field, const float* dev_complex);
+int cupssgb_solver_set_real_pairs_device(cupssgb_solver* s, int field, const float* dev_pairs,
+                                         const float* dev_dealiased_pairs);
 /* Waits for all work queued on the solver's stream. */
 int cupssgb_solver_synchronize(cupssgb_solver* s);
 /* Steps taken so far, kernels launched so far, device bytes held. */
@@ -196,6 +213,13 @@ int cupssgb_evolver_current_step(const cupssgb_evolver* e);
 int cupssgb_evolver_describe(const cupssgb_evolver* e, char* buf, int buflen);
 /* The solver behind an evolver (valid after prepare), for device-level access. */
 cupssgb_solver* cupssgb_evolver_solver(cupssgb_evolver* e);
+/* field::hasCB / callback (fourier = 0) or hasCBFourier / callbackFourier (fourier = 1),
+ * src/field.cpp:48-86.  The callback receives the evolver, the field as float2 pairs
+ * (real space: N (x, 0) values; Fourier space: N complex values, reference layout) and
+ * sx, sy, sz; device pointers in GPU mode, host pointers when created with
+ * with_cuda = 0.  fn = NULL removes it. */
+typedef void (*cupssgb_callback)(void* evolver, float* field_pairs, int sx, int sy, int sz);
+int cupssgb_evolver_set_callback(cupssgb_evolver* e, const char* field, int fourier, cupssgb_callback fn);
 
 #ifdef __cplusplus
 }

@@ -77,6 +77,7 @@ class RefSolver:
         self.time = 0.0
         self.rng = np.random.default_rng(12345)
         self.callbacks = {}          # name -> fn(real ndarray) applied after normalize
+        self.fourier_callbacks = {}  # name -> fn(complex ndarray) applied after the update
         self.prepared = False
 
     # ---- FFT helpers (unnormalised, like cuFFT C2C) ------------------------------------------
@@ -279,6 +280,9 @@ class RefSolver:
                     fac = (fac + v).astype(np.float32)
                 fac.flat[0] = 1.0            # index 0 is skipped (field_kernels.cu:167)
                 c = (c / fac.astype(self.rdt)).astype(self.cdt)
+        fcb = self.fourier_callbacks.get(self.names[f])
+        if fcb is not None:                 # callbackFourier (src/field.cpp:48-57)
+            c = np.asarray(fcb(c), self.cdt)
         self.comp[f] = c
         if self.needs_alias[f]:
             cd = np.where(self.masks[f], c, 0).astype(self.cdt)

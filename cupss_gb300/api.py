@@ -124,6 +124,50 @@ class Solver:
     def get_real_ptr(self, f, host_ptr):
         capi.check(self.lib.cupssgb_solver_get_real(self.h, f, C.cast(host_ptr, capi._FP)))
 
+    # ---- batches ----
+    def set_members(self, n):
+        capi.check(self.lib.cupssgb_solver_set_members(self.h, int(n)))
+
+    def set_member_term_pres(self, m, f, t, pres):
+        arr, n = capi.pres_array(pres)
+        capi.check(self.lib.cupssgb_solver_set_member_term_pres(self.h, m, f, t, arr, n))
+
+    def set_member_implicit(self, m, f, pres):
+        arr, n = capi.pres_array(pres)
+        capi.check(self.lib.cupssgb_solver_set_member_implicit(self.h, m, f, arr, n))
+
+    def set_member_noise(self, m, f, amp):
+        arr, _ = capi.pres_array([amp])
+        capi.check(self.lib.cupssgb_solver_set_member_noise(self.h, m, f, arr))
+
+    def set_member_seed(self, m, seed):
+        capi.check(self.lib.cupssgb_solver_set_member_seed(self.h, m, int(seed)))
+
+    def set_member_active(self, m, on):
+        capi.check(self.lib.cupssgb_solver_set_member_active(self.h, m, int(bool(on))))
+
+    def reset_member(self, m):
+        capi.check(self.lib.cupssgb_solver_reset_member(self.h, m))
+
+    def member_step(self, m):
+        return capi.check(self.lib.cupssgb_solver_member_step(self.h, m))
+
+    def set_real_member(self, f, m, arr):
+        a = np.ascontiguousarray(np.asarray(arr, np.float32).reshape(-1))
+        assert a.size == self.N
+        capi.check(self.lib.cupssgb_solver_set_real_member(self.h, f, m, capi.fptr(a)))
+
+    def get_real_member(self, f, m):
+        out = np.empty(self.N, np.float32)
+        capi.check(self.lib.cupssgb_solver_get_real_member(self.h, f, m, capi.fptr(out)))
+        return out.reshape(self.shape)
+
+    def tune_report(self):
+        n = capi.check(self.lib.cupssgb_solver_tune_report(self.h, None, 0))
+        buf = C.create_string_buffer(n + 1)
+        self.lib.cupssgb_solver_tune_report(self.h, buf, n + 1)
+        return json.loads(buf.value.decode())
+
     @property
     def step_count(self):
         return self.lib.cupssgb_solver_step_count(self.h)
@@ -254,4 +298,84 @@ class Evolver:
         n = self.lib.cupssgb_evolver_describe(self.h, None, 0)
         buf = C.create_string_buffer(n + 1)
         self.lib.cupssgb_evolver_describe(self.h, buf, n + 1)
+        return json.loads(buf.value.decode())
+
+
+class Ensemble:
+    """Mirror of the C++ ``ensemble`` (include/cupss/ensemble.h): one system declared
+    with the evolver's calls, many members (grid, dt, seed, parameter values) advanced
+    together in batch solvers."""
+
+    def __init__(self):
+        self.lib = capi.load()
+        h = C.c_void_p()
+        capi.check(self.lib.cupssgb_ensemble_create(C.byref(h)))
+        self.h = h
+        self.shapes = []
+
+    def close(self):
+        if self.h:
+            self.lib.cupssgb_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def createField(self, name, dynamic):
+        return capi.check(self.lib.cupssgb_ensemble_create_field(self.h, name.encode(), int(bool(dynamic))))
+
+    def addParameter(self, name, value):
+        return capi.check(self.lib.cupssgb_ensemble_add_parameter(self.h, name.encode(), float(value)))
+
+    def addEquation(self, eq):
+        return capi.check(self.lib.cupssgb_ensemble_add_equation(self.h, eq.encode()))
+
+    def addNoise(self, name, amp):
+        return capi.check(self.lib.cupssgb_ensemble_add_noise(self.h, name.encode(), amp.encode()))
+
+    def addMember(self, sx, sy=1, sz=1, dx=1.0, dy=1.0, dz=1.0, dt=0.01, seed=0, **params):
+        m = capi.check(self.lib.cupssgb_ensemble_add_member(self.h, sx, sy, sz, dx, dy, dz, dt, int(seed)))
+        self.shapes.append((sz, sy, sx))
+        for k, v in params.items():
+            self.setMemberParameter(m, k, v)
+        return m
+
+    def setMemberParameter(self, m, name, value):
+        return capi.check(self.lib.cupssgb_ensemble_set_member_parameter(self.h, m, name.encode(), float(value)))
+
+    def prepare(self):
+        return capi.check(self.lib.cupssgb_ensemble_prepare(self.h))
+
+    def setReal(self, m, name, arr):
+        a = np.ascontiguousarray(np.asarray(arr, np.float32).reshape(-1))
+        assert a.size == int(np.prod(self.shapes[m]))
+        return capi.check(self.lib.cupssgb_ensemble_set_real(self.h, m, name.encode(), capi.fptr(a)))
+
+    def advance(self, n):
+        return capi.check(self.lib.cupssgb_ensemble_advance(self.h, int(n)))
+
+    def getReal(self, m, name):
+        out = np.empty(int(np.prod(self.shapes[m])), np.float32)
+        capi.check(self.lib.cupssgb_ensemble_get_real(self.h, m, name.encode(), capi.fptr(out)))
+        return out.reshape(self.shapes[m])
+
+    @property
+    def groups(self):
+        return self.lib.cupssgb_ensemble_groups(self.h)
+
+    @property
+    def device_bytes(self):
+        return self.lib.cupssgb_ensemble_device_bytes(self.h)
+
+    @property
+    def launch_count(self):
+        return self.lib.cupssgb_ensemble_launch_count(self.h)
+
+    def describe(self):
+        n = capi.check(self.lib.cupssgb_ensemble_describe(self.h, None, 0))
+        buf = C.create_string_buffer(n + 1)
+        self.lib.cupssgb_ensemble_describe(self.h, buf, n + 1)
         return json.loads(buf.value.decode())

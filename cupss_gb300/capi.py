@@ -83,6 +83,20 @@ SIGNATURES = {
     "cupssgb_solver_generated_source": (_I, [_P, _I, C.c_char_p, _I]),
     "cupssgb_solver_set_generated_programs": (_I, [_P, _I]),
     "cupssgb_jit_check": (_I, [C.c_char_p, C.c_char_p, _I]),
+    "cupssgb_solver_set_members": (_I, [_P, _I]),
+    "cupssgb_solver_members": (_I, [_P]),
+    "cupssgb_solver_set_member_term_pres": (_I, [_P, _I, _I, _I, _PP, _I]),
+    "cupssgb_solver_set_member_implicit": (_I, [_P, _I, _I, _PP, _I]),
+    "cupssgb_solver_set_member_noise": (_I, [_P, _I, _I, _PP]),
+    "cupssgb_solver_set_member_seed": (_I, [_P, _I, _ULL]),
+    "cupssgb_solver_set_member_active": (_I, [_P, _I, _I]),
+    "cupssgb_solver_reset_member": (_I, [_P, _I]),
+    "cupssgb_solver_member_step": (_LL, [_P, _I]),
+    "cupssgb_solver_set_real_member": (_I, [_P, _I, _I, _FP]),
+    "cupssgb_solver_set_real_member_device": (_I, [_P, _I, _I, _P]),
+    "cupssgb_solver_get_real_member": (_I, [_P, _I, _I, _FP]),
+    "cupssgb_solver_get_real_member_device": (_I, [_P, _I, _I, _P]),
+    "cupssgb_solver_tune_report": (_I, [_P, C.c_char_p, _I]),
     "cupssgb_real_to_fourier_noalloc": (_I, [_P, _P, _I, _I, _I, _P]),
     "cupssgb_host_alloc": (_I, [_LL, C.POINTER(_P)]),
     "cupssgb_host_free": (_I, [_P]),
@@ -107,6 +121,22 @@ SIGNATURES = {
     "cupssgb_evolver_describe": (_I, [_P, C.c_char_p, _I]),
     "cupssgb_evolver_solver": (_P, [_P]),
     "cupssgb_evolver_set_callback": (_I, [_P, _S, _I, CALLBACK]),
+    "cupssgb_ensemble_create": (_I, [C.POINTER(_P)]),
+    "cupssgb_ensemble_destroy": (_I, [_P]),
+    "cupssgb_ensemble_create_field": (_I, [_P, _S, _I]),
+    "cupssgb_ensemble_add_parameter": (_I, [_P, _S, _F]),
+    "cupssgb_ensemble_add_equation": (_I, [_P, _S]),
+    "cupssgb_ensemble_add_noise": (_I, [_P, _S, _S]),
+    "cupssgb_ensemble_add_member": (_I, [_P, _I, _I, _I, _F, _F, _F, _F, _ULL]),
+    "cupssgb_ensemble_set_member_parameter": (_I, [_P, _I, _S, _F]),
+    "cupssgb_ensemble_prepare": (_I, [_P]),
+    "cupssgb_ensemble_set_real": (_I, [_P, _I, _S, _FP]),
+    "cupssgb_ensemble_advance": (_I, [_P, _I]),
+    "cupssgb_ensemble_get_real": (_I, [_P, _I, _S, _FP]),
+    "cupssgb_ensemble_groups": (_I, [_P]),
+    "cupssgb_ensemble_device_bytes": (_LL, [_P]),
+    "cupssgb_ensemble_launch_count": (_LL, [_P]),
+    "cupssgb_ensemble_describe": (_I, [_P, C.c_char_p, _I]),
 }
 
 _lib = None

@@ -1,4 +1,5 @@
 // C-ABI entry points (declared in include/cupss_gb300.h).
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <sstream>
@@ -6,6 +7,7 @@
 #include <vector>
 
 #include "../../include/cupss.h"
+#include "../../include/cupss/ensemble.h"
 #include "../../include/cupss_gb300.h"
 #include "engine.h"
 #include "host_common.h"
@@ -17,6 +19,10 @@ struct cupssgb_solver {
 
 struct cupssgb_evolver {
   evolver* e;
+};
+
+struct cupssgb_ensemble {
+  ensemble* e;
 };
 
 namespace {
@@ -36,11 +42,23 @@ int guard(F&& fn) {
     return fail(e.code, e.what());
   } catch (const cupssgb_host::ParseError& e) {
     return fail(CUPSSGB_ERR_PARSE, e.what());
+  } catch (const cupssgb_host::CapiError& e) {
+    return fail(e.code, e.what());
   } catch (const std::exception& e) {
     return fail(CUPSSGB_ERR_INVALID, e.what());
   } catch (...) {
     return fail(CUPSSGB_ERR_INVALID, "unknown error");
   }
+}
+
+// Writes at most buflen-1 chars of r plus a NUL; returns the full length.
+int copy_out(const std::string& r, char* buf, int buflen) {
+  if (buf && buflen > 0) {
+    const size_t n = std::min((size_t)buflen - 1, r.size());
+    std::memcpy(buf, r.data(), n);
+    buf[n] = 0;
+  }
+  return (int)r.size();
 }
 
 std::vector<cupssgb::HostPres> to_host(const cupssgb_pres* p, int n) {
@@ -592,6 +610,228 @@ int cupssgb_evolver_set_callback(cupssgb_evolver* e, const char* name, int fouri
     }
     return 0;
   });
+}
+
+/* ---------------- batches ---------------- */
+
+int cupssgb_solver_set_members(cupssgb_solver* s, int n) {
+  NEED(s);
+  return guard([&] {
+    s->s->set_members(n);
+    return 0;
+  });
+}
+
+int cupssgb_solver_members(const cupssgb_solver* s) { return s ? s->s->members() : CUPSSGB_ERR_INVALID; }
+
+int cupssgb_solver_set_member_term_pres(cupssgb_solver* s, int member, int field, int term, const cupssgb_pres* pres,
+                                        int n) {
+  NEED(s);
+  if (n > 0) NEED(pres);
+  return guard([&] {
+    s->s->set_member_term_pres(member, field, term, to_host(pres, n));
+    return 0;
+  });
+}
+
+int cupssgb_solver_set_member_implicit(cupssgb_solver* s, int member, int field, const cupssgb_pres* pres, int n) {
+  NEED(s);
+  if (n > 0) NEED(pres);
+  return guard([&] {
+    s->s->set_member_implicit(member, field, to_host(pres, n));
+    return 0;
+  });
+}
+
+int cupssgb_solver_set_member_noise(cupssgb_solver* s, int member, int field, const cupssgb_pres* amp) {
+  NEED(s);
+  NEED(amp);
+  return guard([&] {
+    s->s->set_member_noise(member, field, to_host(amp, 1)[0]);
+    return 0;
+  });
+}
+
+int cupssgb_solver_set_member_seed(cupssgb_solver* s, int member, unsigned long long seed) {
+  NEED(s);
+  return guard([&] {
+    s->s->set_member_seed(member, seed);
+    return 0;
+  });
+}
+
+int cupssgb_solver_set_member_active(cupssgb_solver* s, int member, int active) {
+  NEED(s);
+  return guard([&] {
+    s->s->set_member_active(member, active != 0);
+    return 0;
+  });
+}
+
+int cupssgb_solver_reset_member(cupssgb_solver* s, int member) {
+  NEED(s);
+  return guard([&] {
+    s->s->reset_member(member);
+    return 0;
+  });
+}
+
+long long cupssgb_solver_member_step(cupssgb_solver* s, int member) {
+  if (!s) return fail(CUPSSGB_ERR_INVALID, "null handle");
+  long long out = 0;
+  const int rc = guard([&] {
+    out = s->s->member_step(member);
+    return 0;
+  });
+  return rc != 0 ? rc : out;
+}
+
+int cupssgb_solver_set_real_member(cupssgb_solver* s, int field, int member, const float* host_real) {
+  NEED(s);
+  NEED(host_real);
+  return guard([&] {
+    s->s->set_real(field, host_real, false, member);
+    s->s->synchronize();
+    return 0;
+  });
+}
+
+int cupssgb_solver_set_real_member_device(cupssgb_solver* s, int field, int member, const float* dev_real) {
+  NEED(s);
+  NEED(dev_real);
+  return guard([&] {
+    s->s->set_real(field, dev_real, true, member);
+    return 0;
+  });
+}
+
+int cupssgb_solver_get_real_member(cupssgb_solver* s, int field, int member, float* host_real) {
+  NEED(s);
+  NEED(host_real);
+  return guard([&] {
+    s->s->get_real(field, host_real, false, member);
+    return 0;
+  });
+}
+
+int cupssgb_solver_get_real_member_device(cupssgb_solver* s, int field, int member, float* dev_real) {
+  NEED(s);
+  NEED(dev_real);
+  return guard([&] {
+    s->s->get_real(field, dev_real, true, member);
+    return 0;
+  });
+}
+
+int cupssgb_solver_tune_report(cupssgb_solver* s, char* buf, int buflen) {
+  NEED(s);
+  std::string r;
+  const int rc = guard([&] {
+    r = s->s->tune_report();
+    return 0;
+  });
+  if (rc != 0) return rc;
+  return copy_out(r, buf, buflen);
+}
+
+/* ---------------- ensembles ---------------- */
+
+int cupssgb_ensemble_create(cupssgb_ensemble** out) {
+  NEED(out);
+  return guard([&] {
+    *out = new cupssgb_ensemble{new ensemble()};
+    return 0;
+  });
+}
+
+int cupssgb_ensemble_destroy(cupssgb_ensemble* e) {
+  if (!e) return 0;
+  return guard([&] {
+    delete e->e;
+    delete e;
+    return 0;
+  });
+}
+
+int cupssgb_ensemble_create_field(cupssgb_ensemble* e, const char* name, int dynamic) {
+  NEED(e);
+  NEED(name);
+  return guard([&] { return e->e->createField(name, dynamic != 0); });
+}
+
+int cupssgb_ensemble_add_parameter(cupssgb_ensemble* e, const char* name, float value) {
+  NEED(e);
+  NEED(name);
+  return guard([&] { return e->e->addParameter(name, value); });
+}
+
+int cupssgb_ensemble_add_equation(cupssgb_ensemble* e, const char* equation) {
+  NEED(e);
+  NEED(equation);
+  return guard([&] { return e->e->addEquation(equation); });
+}
+
+int cupssgb_ensemble_add_noise(cupssgb_ensemble* e, const char* field, const char* amplitude) {
+  NEED(e);
+  NEED(field);
+  NEED(amplitude);
+  return guard([&] { return e->e->addNoise(field, amplitude); });
+}
+
+int cupssgb_ensemble_add_member(cupssgb_ensemble* e, int sx, int sy, int sz, float dx, float dy, float dz, float dt,
+                                unsigned long long seed) {
+  NEED(e);
+  return guard([&] { return e->e->addMember(sx, sy, sz, dx, dy, dz, dt, seed); });
+}
+
+int cupssgb_ensemble_set_member_parameter(cupssgb_ensemble* e, int member, const char* name, float value) {
+  NEED(e);
+  NEED(name);
+  return guard([&] { return e->e->setMemberParameter(member, name, value); });
+}
+
+int cupssgb_ensemble_prepare(cupssgb_ensemble* e) {
+  NEED(e);
+  return guard([&] {
+    e->e->prepare();
+    return 0;
+  });
+}
+
+int cupssgb_ensemble_set_real(cupssgb_ensemble* e, int member, const char* field, const float* host_real) {
+  NEED(e);
+  NEED(field);
+  NEED(host_real);
+  return guard([&] { return e->e->setReal(member, field, host_real); });
+}
+
+int cupssgb_ensemble_advance(cupssgb_ensemble* e, int nsteps) {
+  NEED(e);
+  return guard([&] { return e->e->advance(nsteps); });
+}
+
+int cupssgb_ensemble_get_real(cupssgb_ensemble* e, int member, const char* field, float* host_real) {
+  NEED(e);
+  NEED(field);
+  NEED(host_real);
+  return guard([&] { return e->e->getReal(member, field, host_real); });
+}
+
+int cupssgb_ensemble_groups(const cupssgb_ensemble* e) { return e ? e->e->groups() : CUPSSGB_ERR_INVALID; }
+
+long long cupssgb_ensemble_device_bytes(const cupssgb_ensemble* e) { return e ? e->e->deviceBytes() : 0; }
+
+long long cupssgb_ensemble_launch_count(const cupssgb_ensemble* e) { return e ? e->e->launches() : 0; }
+
+int cupssgb_ensemble_describe(const cupssgb_ensemble* e, char* buf, int buflen) {
+  NEED(e);
+  std::string r;
+  const int rc = guard([&] {
+    r = e->e->describe();
+    return 0;
+  });
+  if (rc != 0) return rc;
+  return copy_out(r, buf, buflen);
 }
 
 }  // extern "C"

@@ -46,6 +46,8 @@ Solver::Solver(int sx, int sy, int sz, float dx, float dy, float dz, float dt)
 
 Solver::~Solver() {
   if (stream_) cudaStreamSynchronize(stream_);
+  for (cudaGraphExec_t& g : graph_)
+    if (g) cudaGraphExecDestroy(g);
   for (cudaEvent_t e : ev_pool_) cudaEventDestroy(e);
   for (void* p : allocs_) cudaFree(p);
   if (stream_) cudaStreamDestroy(stream_);
@@ -66,6 +68,7 @@ void* Solver::dalloc(size_t bytes) {
 
 int Solver::add_field(bool dynamic) {
   if (prepared_) throw Error(kErrState, "add_field after prepare");
+  if (!mfields_.empty()) throw Error(kErrState, "add_field after batch member values were set");
   if ((int)fields_.size() >= kMaxFields) throw Error(kErrLimit, "too many fields");
   HostField f;
   f.dynamic = dynamic;
@@ -78,11 +81,13 @@ void Solver::set_implicit(int f, const std::vector<HostPres>& p) {
   if (prepared_ && p.size() != fields_[f].implicit.size())
     throw Error(kErrState, "the number of implicit prefactors cannot change after prepare");
   fields_[f].implicit = p;
+  invalidate_graphs();
 }
 
 int Solver::add_term(int f, const std::vector<int>& product, const std::vector<HostPres>& p) {
   if (f < 0 || f >= nfields()) throw Error(kErrInvalid, "bad field index");
   if (prepared_) throw Error(kErrState, "add_term after prepare");
+  if (!mfields_.empty()) throw Error(kErrState, "add_term after batch member values were set");
   if (p.empty()) throw Error(kErrInvalid, "term without prefactors");
   for (int g : product)
     if (g < 0 || g >= nfields()) throw Error(kErrInvalid, "bad product field index");
@@ -100,15 +105,22 @@ void Solver::set_term_pres(int f, int t, const std::vector<HostPres>& p) {
   if (p.size() != fields_[f].terms[t].pres.size())
     throw Error(kErrInvalid, "prefactor count of a term cannot change");
   fields_[f].terms[t].pres = p;
+  invalidate_graphs();
 }
 
 void Solver::set_noise(int f, bool on, const HostPres& amp) {
   if (f < 0 || f >= nfields()) throw Error(kErrInvalid, "bad field index");
+  if (prepared_ && on != fields_[f].noisy) throw Error(kErrState, "noise cannot be switched after prepare");
   fields_[f].noisy = on;
   fields_[f].noise = amp;
+  invalidate_graphs();
 }
 
-void Solver::set_dt(float dt) { dt_ = dt; }
+void Solver::set_dt(float dt) {
+  dt_ = dt;
+  invalidate_graphs();
+  if (batch_ && prepared_) mvals_dirty_ = true;   // noise bases depend on dt
+}
 
 void Solver::build_plan() {
   const int F = nfields();
@@ -123,6 +135,7 @@ void Solver::build_plan() {
   for (int ph = 0; ph < 2; ++ph) {
     Phase& P = phases_[ph];
     P = Phase();
+    P.id = ph;
     for (int f = 0; f < F; ++f)
       if ((int)fields_[f].dynamic == ph) P.fields.push_back(f);
     for (int f : P.fields) {
@@ -166,7 +179,9 @@ void Solver::prepare() {
   check(cudaGetDevice(&dev), "cudaGetDevice");
   check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
   build_plan();
-  const size_t half = (size_t)Lx_ * sy_ * sz_;
+  half_ = (size_t)Lx_ * sy_ * sz_;
+  const size_t half = half_;
+  const size_t hall = half_ * (size_t)nmem_;   // all members
   const int F = nfields();
   // twiddle super-table: table for length L at offset L, L = 1..2048
   {
@@ -188,20 +203,28 @@ void Solver::prepare() {
   chanz_.assign(F, nullptr);
   par_.assign(F, 0);
   for (int f = 0; f < F; ++f) {
-    state_[0][f] = (float2*)dalloc(half * sizeof(float2));
-    state_[1][f] = (float2*)dalloc(half * sizeof(float2));
+    state_[0][f] = (float2*)dalloc(hall * sizeof(float2));
+    state_[1][f] = (float2*)dalloc(hall * sizeof(float2));
     if (alias_order_[f] > 1) {
-      chan_[f] = (float2*)dalloc(half * sizeof(float2));
-      if (dim_ == 3) chanz_[f] = (float2*)dalloc(half * sizeof(float2));
+      chan_[f] = (float2*)dalloc(hall * sizeof(float2));
+      if (dim_ == 3) chanz_[f] = (float2*)dalloc(hall * sizeof(float2));
     }
   }
   for (Phase& P : phases_)
     for (size_t j = 0; j < P.products.size(); ++j)
-      P.prodbuf.push_back((float2*)dalloc(half * sizeof(float2)));
+      P.prodbuf.push_back((float2*)dalloc(hall * sizeof(float2)));
   scratch_real_ = (float*)dalloc(npoints() * sizeof(float));
   scratch_spec_ = (float2*)dalloc(half * sizeof(float2));
+  if (batch_) {
+    members_d_ = (MemberK*)dalloc((size_t)nmem_ * sizeof(MemberK));
+    for (int ph = 0; ph < 2; ++ph) mvals_d_[ph] = (float*)dalloc((size_t)nmem_ * kMemberVals * sizeof(float));
+    check(cudaMemcpyAsync(members_d_, members_h_.data(), (size_t)nmem_ * sizeof(MemberK), cudaMemcpyHostToDevice,
+                          stream_),
+          "member upload");
+  }
   check(cudaStreamSynchronize(stream_), "prepare sync");
   prepared_ = true;
+  if (batch_) upload_member_values();
   if (use_jit_) {
     // compile the specialised update programs now, not inside the first step
     const int L = (dim_ == 3) ? sz_ : sy_;
@@ -215,6 +238,7 @@ void Solver::prepare() {
       jit_kernel(turn_source(P, p, L, nl), "cupssgb_turn");
     }
   }
+  if (batch_) autotune();
 }
 
 int Solver::pick_w(int L, int nl, int nslots) const {
@@ -249,7 +273,7 @@ void Solver::fill_line_common(LineParams& p, int L, int geo, int mode) const {
   p.tw = tw_;
 }
 
-void Solver::line_fwd_inv(int geo, int mode, const float2* in, float2* out, int xlimit) {
+void Solver::line_fwd_inv(int geo, int mode, const float2* in, float2* out, int xlimit, bool batch) {
   LineParams p;
   const int L = (geo == kGeoY3 || geo == kGeoCol) ? sy_ : sz_;
   fill_line_common(p, L, geo, mode);
@@ -258,19 +282,24 @@ void Solver::line_fwd_inv(int geo, int mode, const float2* in, float2* out, int 
   p.prod_in[0] = in;
   p.prod_out[0] = out;
   p.inv_xlimit[0] = xlimit;
-  dim3 grid((Lx_ + p.W - 1) / p.W, geo == kGeoY3 ? sz_ : (geo == kGeoZ3 ? sy_ : 1));
+  if (batch) {
+    p.mstride = half_;
+    p.members = members_d_;
+  }
+  dim3 grid((Lx_ + p.W - 1) / p.W, geo == kGeoY3 ? sz_ : (geo == kGeoZ3 ? sy_ : 1), batch ? nmem_ : 1);
   check(launch_line_pass(p, 1, 1, grid, stream_), "line pass");
   ++launches_;
 }
 
-void Solver::set_real(int f, const float* src, bool on_device) {
+void Solver::set_real(int f, const float* src, bool on_device, int m) {
   if (!prepared_) throw Error(kErrState, "set_real before prepare");
   if (f < 0 || f >= nfields()) throw Error(kErrInvalid, "bad field index");
+  check_member(m);
   const size_t n = npoints();
   check(cudaMemcpyAsync(scratch_real_, src, n * sizeof(float),
                         on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream_),
         "set_real copy");
-  float2* st = state_[par_[f]][f];
+  float2* st = state_[par_[f]][f] + (size_t)m * half_;
   XParams x;
   std::memset(&x, 0, sizeof(x));
   x.Lx = Lx_;
@@ -295,8 +324,8 @@ void Solver::set_real(int f, const float* src, bool on_device) {
   }
 }
 
-void Solver::to_real_scratch(int f) {
-  const float2* st = state_[par_[f]][f];
+void Solver::to_real_scratch(int f, int m) {
+  const float2* st = state_[par_[f]][f] + (size_t)m * half_;
   const float2* spec = st;
   if (dim_ == 3) {
     line_fwd_inv(kGeoZ3, kModeInv, st, scratch_spec_, Lx_);
@@ -324,10 +353,11 @@ void Solver::to_real_scratch(int f) {
   ++launches_;
 }
 
-void Solver::get_real(int f, float* dst, bool on_device) {
+void Solver::get_real(int f, float* dst, bool on_device, int m) {
   if (!prepared_) throw Error(kErrState, "get_real before prepare");
   if (f < 0 || f >= nfields()) throw Error(kErrInvalid, "bad field index");
-  to_real_scratch(f);
+  check_member(m);
+  to_real_scratch(f, m);
   check(cudaMemcpyAsync(dst, scratch_real_, npoints() * sizeof(float),
                         on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, stream_),
         "get_real copy");
@@ -446,13 +476,15 @@ void Solver::set_real_pairs_device(int f, const float2* real, const float2* deal
 void Solver::advance_phase(int phase) {
   if (!prepared_) throw Error(kErrState, "advance before prepare");
   if (phase < 0 || phase > 1) throw Error(kErrInvalid, "phase is 0 (non-dynamic) or 1 (dynamic)");
+  if (batch_) throw Error(kErrUnsupported, "phase-wise stepping (callbacks) is for single systems");
   run_phase(phases_[phase]);
   if (phase == 1) ++step_;
 }
 
-void Solver::get_fourier(int f, float2* dst, bool on_device) {
+void Solver::get_fourier(int f, float2* dst, bool on_device, int m) {
   if (!prepared_) throw Error(kErrState, "get_fourier before prepare");
   if (f < 0 || f >= nfields()) throw Error(kErrInvalid, "bad field index");
+  check_member(m);
   float2* out = dst;
   if (!on_device) {
     if (!scratch_full_) scratch_full_ = (float2*)dalloc(npoints() * sizeof(float2));
@@ -463,7 +495,7 @@ void Solver::get_fourier(int f, float2* dst, bool on_device) {
   e.sy = sy_;
   e.sz = sz_;
   e.Lx = Lx_;
-  e.spec = state_[par_[f]][f];
+  e.spec = state_[par_[f]][f] + (size_t)m * half_;
   e.full = out;
   check(launch_expand(e, stream_), "expand spectrum");
   ++launches_;
@@ -479,7 +511,9 @@ void Solver::synchronize() {
   if (stream_) check(cudaStreamSynchronize(stream_), "synchronize");
 }
 
-void Solver::fill_turn(const Phase& P, LineParams& p, int& nslots, bool& any_chan) const {
+void Solver::fill_turn(const Phase& P, LineParams& p, int& nslots, bool& any_chan,
+                       const std::vector<HostField>* fields) const {
+  const std::vector<HostField>& FS = fields ? *fields : fields_;
   const int geo = (dim_ == 3) ? kGeoZ3 : kGeoCol;
   const int L = (dim_ == 3) ? sz_ : sy_;
   const bool have_dev = prepared_;
@@ -495,7 +529,7 @@ void Solver::fill_turn(const Phase& P, LineParams& p, int& nslots, bool& any_cha
   int nt = 0, npres = 0, ts = 0;
   for (int fi = 0; fi < p.nf; ++fi) {
     const int f = P.fields[fi];
-    const HostField& hf = fields_[f];
+    const HostField& hf = FS[f];
     FieldK& K = p.f[fi];
     K.cur = have_dev ? state_[par_[f]][f] : nullptr;
     K.next = have_dev ? state_[par_[f] ^ 1][f] : nullptr;
@@ -600,9 +634,10 @@ const std::string& Solver::turn_source(Phase& P, const LineParams& p, int L, int
     sig.insert(sig.end(), {q.q2n, q.iqx, q.iqy, q.iqz, q.invq});
   }
   sig.push_back(turn_min_blocks_);
+  sig.push_back(batch_ ? 1 : 0);
   if (sig != P.jit_sig) {
     P.jit_sig = sig;
-    P.jit_src = jit_generate_turn(p, L, nl, turn_min_blocks_);
+    P.jit_src = jit_generate_turn(p, L, nl, turn_min_blocks_, batch_);
   }
   return P.jit_src;
 }
@@ -618,7 +653,7 @@ std::vector<std::string> Solver::generated_sources() {
     int nslots = 0;
     bool any_chan = false;
     fill_turn(P, p, nslots, any_chan);
-    out.push_back(jit_generate_turn(p, L, nl));
+    out.push_back(jit_generate_turn(p, L, nl, turn_min_blocks_, batch_));
   }
   return out;
 }
@@ -646,14 +681,18 @@ void Solver::run_phase(Phase& P) {
       }
     }
     x.tw = tw_;
+    if (batch_) {
+      x.mstride = half_;
+      x.members = members_d_;
+    }
     mark_begin();
-    check(launch_row_pass(x, stream_), "row pass");
+    check(launch_row_pass(x, stream_, batch_ ? nmem_ : 1), "row pass");
     mark_end("row_pass");
     ++launches_;
     if (dim_ == 3) {
       for (size_t q = 0; q < P.products.size(); ++q) {
         mark_begin();
-        line_fwd_inv(kGeoY3, kModeFwd, P.prodbuf[q], P.prodbuf[q], Lx_);
+        line_fwd_inv(kGeoY3, kModeFwd, P.prodbuf[q], P.prodbuf[q], Lx_, batch_);
         mark_end("line_fwd_y");
       }
     }
@@ -668,7 +707,13 @@ void Solver::run_phase(Phase& P) {
   fill_turn(P, p, nslots, any_chan);
   p.W = pick_w(L, nl, nslots);
   if (turn_w_ > 0 && turn_w_ < p.W) p.W = turn_w_;
-  dim3 grid((Lx_ + p.W - 1) / p.W, dim_ == 3 ? std::max(sy_ / 2, 1) : 1);
+  if (batch_) {
+    if (P.tuned_w > 0) p.W = P.tuned_w;
+    p.mstride = half_;
+    p.members = members_d_;
+    p.mvals = mvals_d_[P.id];
+  }
+  dim3 grid((Lx_ + p.W - 1) / p.W, dim_ == 3 ? std::max(sy_ / 2, 1) : 1, batch_ ? nmem_ : 1);
   mark_begin();
   if (use_jit_) {
     const std::string& src = turn_source(P, p, L, nl);
@@ -687,7 +732,7 @@ void Solver::run_phase(Phase& P) {
     for (int f : P.fields)
       if (alias_order_[f] > 1) {
         mark_begin();
-        line_fwd_inv(kGeoY3, kModeInv, chanz_[f], chan_[f], sx_ / (alias_order_[f] + 1));
+        line_fwd_inv(kGeoY3, kModeInv, chanz_[f], chan_[f], sx_ / (alias_order_[f] + 1), batch_);
         mark_end("line_inv_y");
       }
   }
@@ -772,13 +817,24 @@ double Solver::time_advance(int nsteps) {
   return ms;
 }
 
+void Solver::step_once() {
+  run_phase(phases_[0]);
+  run_phase(phases_[1]);
+  if (batch_) {
+    check(launch_tick(members_d_, nmem_, stream_), "member step count");
+    ++launches_;
+  }
+  ++step_;
+}
+
 void Solver::advance(int nsteps) {
   if (!prepared_) throw Error(kErrState, "advance before prepare");
-  for (int s = 0; s < nsteps; ++s) {
-    run_phase(phases_[0]);
-    run_phase(phases_[1]);
-    ++step_;
+  if (batch_) {
+    if (mvals_dirty_) upload_member_values();
+    if (!timing_)
+      for (; nsteps >= kGraphSteps; nsteps -= kGraphSteps) run_graph();
   }
+  for (int s = 0; s < nsteps; ++s) step_once();
 }
 
 }  // namespace cupssgb

@@ -68,10 +68,31 @@ class Solver {
 
   void prepare();
   bool prepared() const { return prepared_; }
-  void set_real(int f, const float* src, bool src_on_device);
+  // m: batch member (0 for a single system)
+  void set_real(int f, const float* src, bool src_on_device, int m = 0);
   void advance(int nsteps);
-  void get_real(int f, float* dst, bool dst_on_device);
-  void get_fourier(int f, float2* dst, bool dst_on_device);
+  void get_real(int f, float* dst, bool dst_on_device, int m = 0);
+  void get_fourier(int f, float2* dst, bool dst_on_device, int m = 0);
+
+  // ---- batches: n independent systems of this structure and grid in one solver ----
+  // set_members(n) before prepare turns the solver into a batch.  Member 0 starts as the
+  // system given by the add_* calls and members 1..n-1 as copies of it; each member can
+  // then get its own prefactor values (same monomials), noise amplitude and seed.  Every
+  // step launch covers all members (blockIdx.z = member); a member's noise counter is
+  // its own step count, so its trajectory does not depend on the rest of the batch.
+  // Steps are replayed from CUDA graphs of kGraphSteps steps.
+  void set_members(int n);
+  int members() const { return nmem_; }
+  bool batched() const { return batch_; }
+  void set_member_term_pres(int m, int f, int t, const std::vector<HostPres>& p);
+  void set_member_implicit(int m, int f, const std::vector<HostPres>& p);
+  void set_member_noise(int m, int f, const HostPres& amp);
+  void set_member_seed(int m, uint64_t seed);
+  void set_member_active(int m, bool on);     // inactive members are skipped by every launch
+  void reset_member(int m);                   // zero states and copies, step count 0
+  long long member_step(int m);
+  std::string tune_report() const;            // JSON: autotuned launch shapes per phase
+  static constexpr int kGraphSteps = 16;
   void get_real_pairs_device(int f, float2* dst);   // reference float2 layout (x, 0)
   // Materialisation points for callbacks (src/field.cpp:48-86), all device pointers in
   // the reference's layouts, ordered on the solver's stream:
@@ -107,6 +128,7 @@ class Solver {
 
  private:
   struct Phase {
+    int id = 0;                              // 0: non-dynamic, 1: dynamic
     std::vector<int> fields;                 // fields updated in this phase
     std::vector<std::vector<int>> products;  // sorted multisets (size >= 2)
     std::vector<int> xin;                    // fields feeding the row pass
@@ -114,18 +136,30 @@ class Solver {
     std::vector<int> term_slot;              // per (field, term) flattened: product slot or -1
     std::vector<int> jit_sig;                // structure of the last generated update program
     std::string jit_src;
+    int tuned_w = 0;                         // batches: autotuned turnaround tile width
+    std::vector<std::pair<int, double>> tune_ms;   // candidate W -> ms per launch
   };
 
   void check(cudaError_t e, const char* what);
   void* dalloc(size_t bytes);
   void build_plan();
   void run_phase(Phase& ph);
-  void fill_turn(const Phase& P, LineParams& p, int& nslots, bool& any_chan) const;
+  void fill_turn(const Phase& P, LineParams& p, int& nslots, bool& any_chan,
+                 const std::vector<HostField>* fields = nullptr) const;
   const std::string& turn_source(Phase& P, const LineParams& p, int L, int nl);
   void fill_line_common(LineParams& p, int L, int geo, int mode) const;
   int pick_w(int L, int nl, int nslots) const;
-  void line_fwd_inv(int geo, int mode, const float2* in, float2* out, int xlimit);
-  void to_real_scratch(int f);
+  void line_fwd_inv(int geo, int mode, const float2* in, float2* out, int xlimit, bool batch = false);
+  void to_real_scratch(int f, int m);
+  void step_once();
+  // batches
+  void check_member(int m) const;
+  void check_same_monomials(const std::vector<HostPres>& a, const std::vector<HostPres>& b) const;
+  void upload_member_values();
+  void autotune();
+  void zero_dynamic_buffers();
+  void invalidate_graphs();
+  void run_graph();
   void row_pass_simple(int in_mode, const void* in, int out_mode, void* out, float scale);
   void forward_lines(float2* st);
   void channel_from_state(int f, float2* dst);
@@ -146,6 +180,17 @@ class Solver {
   long long step_ = 0;
   long long launches_ = 0;
   size_t dev_bytes_ = 0;
+  // batches
+  int nmem_ = 1;
+  bool batch_ = false;
+  size_t half_ = 0;                              // elements of one member's spectrum
+  std::vector<std::vector<HostField>> mfields_;  // per member (values only differ)
+  std::vector<MemberK> members_h_;
+  MemberK* members_d_ = nullptr;
+  float* mvals_d_[2] = {nullptr, nullptr};
+  bool mvals_dirty_ = false;
+  cudaGraphExec_t graph_[2] = {nullptr, nullptr};   // by parity of the step count
+  long long graph_launches_ = 0;                     // kernels per graph replay
 
   cudaStream_t stream_ = nullptr;
   float2* tw_ = nullptr;

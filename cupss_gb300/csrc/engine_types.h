@@ -63,6 +63,17 @@ struct FieldK {
   int self_src;          // prefetch slot of the own state, or -1
 };
 
+// One member of a batch: a solver can hold several independent systems of the same
+// structure and grid, member z at blockIdx.z of every step launch.  Each member has
+// its own Philox key, its own step count (the noise counter) and an active flag (an
+// inactive member is skipped by every kernel and does not count steps).
+struct MemberK {
+  uint32_t key0, key1, step, active;
+};
+// Per-member numerical values of one phase: [k] = pres[k].pre for k < kMaxPres,
+// [kMaxPres + fi] = f[fi].noise_base.
+constexpr int kMemberVals = kMaxPres + kMaxPhaseFields;
+
 enum LineGeo : int {
   kGeoCol = 0,   // 1D/2D: lines are y-columns, elem = y*Lx + kx'
   kGeoY3 = 1,    // 3D y lines, elem = (z*sy + y)*Lx + kx', blockIdx.y = z
@@ -88,6 +99,11 @@ struct LineParams {
   const float2* state[kMaxFields];  // current state of every field
   uint32_t key0, key1, step;
   const float2* tw;
+  // batches: member z's arrays start z * mstride elements after every pointer above;
+  // members / mvals are null for a single system (key, step and values above)
+  size_t mstride;
+  const MemberK* members;
+  const float* mvals;               // [member][kMemberVals]
 };
 
 enum XInMode : int { kXInSpectral = 0, kXInReal = 1, kXInRealPair = 2 };   // RealPair: float2 (x, y) reads .x
@@ -104,6 +120,8 @@ struct XParams {
   int prod_n[kMaxProd];
   int prod_f[kMaxProd][kMaxOrder];
   const float2* tw;
+  size_t mstride;                   // batches: member z's rows start z * mstride elements on
+  const MemberK* members;           // null for a single system
 };
 
 struct ExpandParams {

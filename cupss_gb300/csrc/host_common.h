@@ -11,4 +11,10 @@ struct ParseError : std::runtime_error {
   explicit ParseError(const std::string& m) : std::runtime_error(m) {}
 };
 
+// A failed C-ABI call made by a host class, with its status code.
+struct CapiError : std::runtime_error {
+  int code;
+  CapiError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
 }  // namespace cupssgb_host

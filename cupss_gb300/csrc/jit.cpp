@@ -52,7 +52,15 @@ std::string keep_expr(int s, const PresK& p, bool* never) {
 
 }  // namespace
 
-std::string jit_generate_turn(const LineParams& p, int L, int NL, int min_blocks) {
+std::string jit_generate_turn(const LineParams& p, int L, int NL, int min_blocks, bool batched) {
+  // numerical values: the parameter block (one system) or the batch member's row
+  auto pre = [&](int k) {
+    return batched ? "__ldg(mv + " + std::to_string(k) + ")" : "P.pres[" + std::to_string(k) + "].pre";
+  };
+  auto nbase = [&](int fi) {
+    return batched ? "__ldg(mv + kMaxPres + " + std::to_string(fi) + ")"
+                   : "P.f[" + std::to_string(fi) + "].noise_base";
+  };
   std::ostringstream o;
   o << "#include \"turn.cuh\"\n"
     << "namespace cupssgb {\n"
@@ -62,6 +70,7 @@ std::string jit_generate_turn(const LineParams& p, int L, int NL, int min_blocks
     << "  __device__ __forceinline__ static float2 eval(const LineParams& P, int fi, const VPoint& vp, "
        "const F& fx) {\n"
     << "    const float q2 = vp.q2;\n"
+    << (batched ? "    const float* mv = P.mvals + (size_t)blockIdx.z * kMemberVals;\n" : "")
     << "    switch (fi) {\n";
   for (int fi = 0; fi < p.nf; ++fi) {
     const FieldK& K = p.f[fi];
@@ -86,7 +95,7 @@ std::string jit_generate_turn(const LineParams& p, int L, int NL, int min_blocks
         const std::string keep = keep_expr(T.s, pr, &never);
         if (never) continue;
         std::ostringstream term;
-        term << "P.pres[" << T.pres0 + j << "].pre" << pow_expr("q2", pr.q2n) << pow_expr("vp.qx", pr.iqx)
+        term << pre(T.pres0 + j) << pow_expr("q2", pr.q2n) << pow_expr("vp.qx", pr.iqx)
              << pow_expr("vp.qy", pr.iqy) << pow_expr("vp.qz", pr.iqz) << pow_expr("iq", pr.invq);
         if (keep.empty()) o << "          mt += " << term.str() << ";\n";
         else o << "          if " << keep << " mt += " << term.str() << ";\n";
@@ -102,7 +111,7 @@ std::string jit_generate_turn(const LineParams& p, int L, int NL, int min_blocks
     }
     std::ostringstream amp;
     if (K.noisy) {
-      amp << "P.f[" << fi << "].noise_base";
+      amp << nbase(fi);
       if (K.noise_q2n) amp << "*sqrtf(1.f" << pow_expr("q2", K.noise_q2n) << ")";
       if (K.noise_invq) amp << "*sqrtf(1.f" << pow_expr("iq", K.noise_invq) << ")";
     }
@@ -110,7 +119,7 @@ std::string jit_generate_turn(const LineParams& p, int L, int NL, int min_blocks
     std::ostringstream imp;
     for (int j = 0; j < K.nimp; ++j) {
       const PresK& pr = p.pres[K.imp0 + j];
-      imp << (j ? " + " : "") << "P.pres[" << K.imp0 + j << "].pre" << pow_expr("q2", pr.q2n)
+      imp << (j ? " + " : "") << pre(K.imp0 + j) << pow_expr("q2", pr.q2n)
           << pow_expr(K.dynamic ? "iqd" : "iq", pr.invq);
     }
     if (K.dynamic) {

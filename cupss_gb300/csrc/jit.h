@@ -11,7 +11,8 @@ namespace cupssgb {
 // CUDA source of the turnaround kernel `cupssgb_turn` specialised to the update
 // program described by p (its fields, terms and prefactor exponents), L, NL.
 // min_blocks: the minimum resident CTAs per SM requested from the compiler.
-std::string jit_generate_turn(const LineParams& p, int L, int NL, int min_blocks = 2);
+// batched: numerical values come from the batch member's row of P.mvals.
+std::string jit_generate_turn(const LineParams& p, int L, int NL, int min_blocks = 2, bool batched = false);
 // Compiles (once per source text) and returns the kernel handle.  Throws Error.
 cudaKernel_t jit_kernel(const std::string& source, const char* entry);
 // Compiles for sm_103a without loading (no GPU needed); returns "" or the log.

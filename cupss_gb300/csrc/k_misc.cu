@@ -107,6 +107,16 @@ __global__ void mask_spectrum(const MaskParams p) {
   }
 }
 
+__global__ void tick_members(MemberK* m, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && m[i].active) m[i].step += 1u;
+}
+
+cudaError_t launch_tick(MemberK* members, int n, cudaStream_t st) {
+  tick_members<<<(n + 255) / 256, 256, 0, st>>>(members, n);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_compress(const CompressParams& p, cudaStream_t st) {
   const size_t H = (size_t)p.Lx * p.sy * p.sz;
   int blocks = (int)((H + 255) / 256);

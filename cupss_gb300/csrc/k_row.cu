@@ -5,7 +5,7 @@
 namespace cupssgb {
 
 template <int LX>
-static cudaError_t launch_row_t(const XParams& p, cudaStream_t st) {
+static cudaError_t launch_row_t(const XParams& p, cudaStream_t st, int nz) {
   using C = RowCfg<LX>;
   static bool attr = false;
   const size_t smem = (size_t)(1 + p.n_in) * C::RW * C::PL * sizeof(float2);
@@ -16,7 +16,7 @@ static cudaError_t launch_row_t(const XParams& p, cudaStream_t st) {
     attr = true;
   }
   dim3 block(C::M, C::RW);
-  dim3 grid((p.rows + C::RW - 1) / C::RW);
+  dim3 grid((p.rows + C::RW - 1) / C::RW, 1, nz);
   row_pass<LX><<<grid, block, smem, st>>>(p);
   return cudaGetLastError();
 }
@@ -27,19 +27,19 @@ static size_t row_smem_t(int n_in) {
   return (size_t)(1 + n_in) * C::RW * C::PL * sizeof(float2);
 }
 
-cudaError_t launch_row_pass(const XParams& p, cudaStream_t st) {
+cudaError_t launch_row_pass(const XParams& p, cudaStream_t st, int nz) {
   switch (p.Lx) {
-    case 1: return launch_row_t<1>(p, st);
-    case 2: return launch_row_t<2>(p, st);
-    case 4: return launch_row_t<4>(p, st);
-    case 8: return launch_row_t<8>(p, st);
-    case 16: return launch_row_t<16>(p, st);
-    case 32: return launch_row_t<32>(p, st);
-    case 64: return launch_row_t<64>(p, st);
-    case 128: return launch_row_t<128>(p, st);
-    case 256: return launch_row_t<256>(p, st);
-    case 512: return launch_row_t<512>(p, st);
-    case 1024: return launch_row_t<1024>(p, st);
+    case 1: return launch_row_t<1>(p, st, nz);
+    case 2: return launch_row_t<2>(p, st, nz);
+    case 4: return launch_row_t<4>(p, st, nz);
+    case 8: return launch_row_t<8>(p, st, nz);
+    case 16: return launch_row_t<16>(p, st, nz);
+    case 32: return launch_row_t<32>(p, st, nz);
+    case 64: return launch_row_t<64>(p, st, nz);
+    case 128: return launch_row_t<128>(p, st, nz);
+    case 256: return launch_row_t<256>(p, st, nz);
+    case 512: return launch_row_t<512>(p, st, nz);
+    case 1024: return launch_row_t<1024>(p, st, nz);
     default: return cudaErrorInvalidValue;
   }
 }

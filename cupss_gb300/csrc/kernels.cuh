@@ -69,6 +69,7 @@ row_pass(const XParams p) {
   using C = RowCfg<LX>;
   constexpr int M = C::M, R = C::R, PL = C::PL, RW = C::RW;
   extern __shared__ float2 smem[];
+  if (p.members && !p.members[blockIdx.z].active) return;   // CTA-uniform
   const int m = threadIdx.x;
   const int rl = threadIdx.y;
   const int row = blockIdx.x * RW + rl;
@@ -76,7 +77,7 @@ row_pass(const XParams p) {
   const int sx = 2 * LX;
   float2* T = smem + rl * PL;
   auto slot = [&](int i) { return smem + (size_t)(1 + i) * RW * PL + rl * PL; };
-  const size_t rowoff = (size_t)(live ? row : 0) * LX;
+  const size_t rowoff = (size_t)blockIdx.z * p.mstride + (size_t)(live ? row : 0) * LX;
   float2 v[R];
 
   for (int c = 0; c < p.n_in; ++c) {
@@ -182,6 +183,7 @@ __global__ void __launch_bounds__(256, 2)
 line_pass(const LineParams P) {
   constexpr int M = LineCfg<L>::M, R = LineCfg<L>::R;
   extern __shared__ float2 smem[];
+  if (P.members && !P.members[blockIdx.z].active) return;   // CTA-uniform
   const LineGeom<L, 1> g(P);
   float2 v[R];
   for (int c = 0; c < P.n_prod; ++c) {

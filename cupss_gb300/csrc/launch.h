@@ -5,8 +5,8 @@
 
 namespace cupssgb {
 
-// Row pass over all rows; picks the template by p.Lx.
-cudaError_t launch_row_pass(const XParams& p, cudaStream_t st);
+// Row pass over all rows (of nz batch members); picks the template by p.Lx.
+cudaError_t launch_row_pass(const XParams& p, cudaStream_t st, int nz = 1);
 size_t row_pass_smem(int Lx, int n_in);
 
 // Line pass: grid.x = ceil(Lx/W) tiles, grid.y per geometry; nl = 2 for the paired
@@ -18,6 +18,8 @@ int line_threads(int L, int nl, int W);
 cudaError_t launch_expand(const ExpandParams& p, cudaStream_t st);
 cudaError_t launch_compress(const CompressParams& p, cudaStream_t st);
 cudaError_t launch_mask(const MaskParams& p, cudaStream_t st);
+// Batches: advances the step count of every active member by one.
+cudaError_t launch_tick(MemberK* members, int n, cudaStream_t st);
 
 // per-L launchers (one translation unit per group of sizes)
 #define CUPSSGB_DECL_LINE(L) \

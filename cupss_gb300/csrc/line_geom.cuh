@@ -11,7 +11,8 @@
 //             Hermitian partner (-ky, -kz) of every point of the packed column kx' = 0 is
 //             in the same CTA.
 // Shared-memory slots hold NL * PL * W float2, position n of line `line` of column w at
-// (line*PL + pad_pos(n))*W + w.
+// (line*PL + pad_pos(n))*W + w.  In a batch, blockIdx.z is the member and every element
+// index is offset by mbase = blockIdx.z * P.mstride.
 #pragma once
 #include "engine_types.h"
 #include "fft.cuh"
@@ -23,7 +24,7 @@ struct LineGeom {
   static constexpr int PL = padded_len<L>();
   int W, w, m, l, kx0, kxp, lineky;
   bool ok;
-  size_t lbase, pstride, slot_sz;
+  size_t lbase, pstride, slot_sz, mbase;
   __device__ __forceinline__ explicit LineGeom(const LineParams& P) { init(P, blockIdx.x, blockIdx.y); }
   // Explicit tile coordinates (persistent kernels): tx = kx' tile, ty = line index.
   __device__ __forceinline__ LineGeom(const LineParams& P, int tx, int ty) { init(P, tx, ty); }
@@ -55,6 +56,8 @@ struct LineGeom {
       pstride = (size_t)P.sy * Lx;
     }
     ok = (kxp < Lx) && lineok;
+    mbase = (size_t)blockIdx.z * P.mstride;
+    lbase += mbase;
     slot_sz = (size_t)NL * PL * W;
   }
   __device__ __forceinline__ size_t elem(int pos) const { return lbase + (size_t)pos * pstride; }

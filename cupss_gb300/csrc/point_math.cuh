@@ -34,6 +34,20 @@ __device__ __forceinline__ VPoint make_vpoint(const LineParams& P, int kx, int k
   return vp;
 }
 
+// Noise counter inputs of the system a CTA works on: the solver's (single system) or
+// the batch member's (blockIdx.z).
+struct NoiseKey {
+  uint32_t key0, key1, step;
+};
+
+// Numerical value of prefactor k / noise base of phase field fi for this CTA's system.
+__device__ __forceinline__ float pre_val(const LineParams& P, int k) {
+  return P.mvals ? __ldg(P.mvals + (size_t)blockIdx.z * kMemberVals + k) : P.pres[k].pre;
+}
+__device__ __forceinline__ float noise_base_val(const LineParams& P, int fi) {
+  return P.mvals ? __ldg(P.mvals + (size_t)blockIdx.z * kMemberVals + kMaxPres + fi) : P.f[fi].noise_base;
+}
+
 __device__ __forceinline__ float ipow(float x, int n) {
   float r = 1.f;
   for (int i = 0; i < n; ++i) r *= x;
@@ -52,7 +66,7 @@ __device__ __forceinline__ float term_mult(const LineParams& P, const TermK& T, 
     const PresK pr = P.pres[T.pres0 + j];
     const int e = T.s + (vp.nyx ? 0 : pr.iqx) + (vp.nyy ? 0 : pr.iqy) + (vp.nyz ? 0 : pr.iqz);
     if (e & 1) continue;
-    float v = pr.pre;
+    float v = pre_val(P, T.pres0 + j);
     v *= ipow(vp.q2, pr.q2n);
     v *= ipow(vp.qx, pr.iqx);
     v *= ipow(vp.qy, pr.iqy);
@@ -72,7 +86,7 @@ __device__ __forceinline__ float implicit_factor(const LineParams& P, const Fiel
   float acc = F.dynamic ? 1.f : 0.f;
   for (int j = 0; j < F.nimp; ++j) {
     const PresK pr = P.pres[F.imp0 + j];
-    float v = pr.pre;
+    float v = pre_val(P, F.imp0 + j);
     if (pr.q2n != 0) v *= ipow(vp.q2, pr.q2n);
     if (pr.invq != 0) {
       bool nz = F.dynamic ? (vp.kx > 0 || vp.ky > 0) : !vp.origin;
@@ -85,8 +99,9 @@ __device__ __forceinline__ float implicit_factor(const LineParams& P, const Fiel
   return acc;
 }
 
-__device__ __forceinline__ float noise_amp(const FieldK& F, const VPoint& vp) {
-  float a = F.noise_base;
+__device__ __forceinline__ float noise_amp(const LineParams& P, int fi, const VPoint& vp) {
+  const FieldK& F = P.f[fi];
+  float a = noise_base_val(P, fi);
   if (F.noise_q2n != 0) a *= sqrtf(ipow(vp.q2, F.noise_q2n));
   if (F.noise_invq != 0) {
     const float iq = vp.origin ? 0.f : 1.0f / sqrtf(vp.q2);
@@ -109,22 +124,23 @@ __device__ __forceinline__ int line_axis_len(const LineParams& P) {
 }
 
 // Both modes (t, t + Lt/2) of a folded pair, t < Lt/2, 0 < kx < sx/2.
-__device__ __forceinline__ void noise_pair(const LineParams& P, int fid, int kx, int ky, int kz, float2& lo,
-                                           float2& hi) {
+__device__ __forceinline__ void noise_pair(const LineParams& P, const NoiseKey& nk, int fid, int kx, int ky,
+                                           int kz, float2& lo, float2& hi) {
   const uint32_t lin = ((uint32_t)kz * P.sy + ky) * P.sx + kx;
   float g1, g2, g3, g4;
-  philox_normal4(lin, P.step, (uint32_t)fid, P.key0, P.key1, g1, g2, g3, g4);
+  philox_normal4(lin, nk.step, (uint32_t)fid, nk.key0, nk.key1, g1, g2, g3, g4);
   lo = make_float2(P.sqrtHalfN * g1, P.sqrtHalfN * g2);
   hi = make_float2(P.sqrtHalfN * g3, P.sqrtHalfN * g4);
 }
 
 // Any mode with kx <= sx/2.
-__device__ __forceinline__ float2 noise_at(const LineParams& P, int fid, int kx, int ky, int kz) {
+__device__ __forceinline__ float2 noise_at(const LineParams& P, const NoiseKey& nk, int fid, int kx, int ky,
+                                           int kz) {
   if (kx != 0 && 2 * kx != P.sx) {
     const int Lt = line_axis_len(P);
     if (Lt == 1) {
       float2 lo, hi;
-      noise_pair(P, fid, kx, ky, kz, lo, hi);
+      noise_pair(P, nk, fid, kx, ky, kz, lo, hi);
       return lo;
     }
     const int h = Lt / 2;
@@ -132,7 +148,7 @@ __device__ __forceinline__ float2 noise_at(const LineParams& P, int fid, int kx,
     const bool upper = t >= h;
     if (upper) t -= h;
     float2 lo, hi;
-    noise_pair(P, fid, kx, ky, kz, lo, hi);
+    noise_pair(P, nk, fid, kx, ky, kz, lo, hi);
     return upper ? hi : lo;
   }
   const uint32_t lin = ((uint32_t)kz * P.sy + ky) * P.sx + kx;
@@ -146,7 +162,7 @@ __device__ __forceinline__ float2 noise_at(const LineParams& P, int fid, int kx,
     ctr = plin;
     conj = true;
   }
-  philox_normal2(ctr, P.step, (uint32_t)fid, P.key0, P.key1, g1, g2);
+  philox_normal2(ctr, nk.step, (uint32_t)fid, nk.key0, nk.key1, g1, g2);
   if (plin == lin) return make_float2(P.sqrtN * g1, 0.f);
   return make_float2(P.sqrtHalfN * g1, conj ? -P.sqrtHalfN * g2 : P.sqrtHalfN * g2);
 }

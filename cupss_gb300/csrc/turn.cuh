@@ -77,7 +77,7 @@ struct InterpProg {
     float2 nv;
     if (K.dynamic) {
       nv = c_add(fx.src(K.self_src), c_scale(acc, P.dt));
-      if (K.noisy) nv = c_add(nv, c_scale(fx.xi, noise_amp(K, vp)));
+      if (K.noisy) nv = c_add(nv, c_scale(fx.xi, noise_amp(P, fi, vp)));
       if (K.nimp > 0) {
         const float rd = 1.0f / implicit_factor(P, K, vp);
         nv = make_float2(nv.x * rd, nv.y * rd);
@@ -85,7 +85,7 @@ struct InterpProg {
     } else {
       nv = (K.nterms > 0) ? acc : fx.src(K.self_src);
       if (K.noisy) {
-        const float2 nz = c_scale(fx.xi, noise_amp(K, vp));
+        const float2 nz = c_scale(fx.xi, noise_amp(P, fi, vp));
         nv = (K.nterms > 0) ? c_add(nv, nz) : nz;
       }
       if (K.nimp > 0 && !vp.origin) {
@@ -126,6 +126,12 @@ template <int L, int NL, class Prog>
 __device__ __forceinline__ void turn_body(const LineParams& P) {
   constexpr int R = LineCfg<L>::R;
   extern __shared__ float2 smem[];
+  NoiseKey nk{P.key0, P.key1, P.step};
+  if (P.members) {
+    const MemberK mk = P.members[blockIdx.z];
+    if (!mk.active) return;   // CTA-uniform, before any barrier
+    nk = NoiseKey{mk.key0, mk.key1, mk.step};
+  }
   const LineGeom<L, NL> g(P);
   const int m = g.m, l = g.l;
   const size_t slot_sz = g.slot_sz;
@@ -187,8 +193,8 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
             if (lower) {
               const int pos = pos_step2<L>(m, i);
               float2 lo, hi;
-              if (z3) noise_pair(P, F.fid, g.kxp, g.lineky, pos, lo, hi);
-              else noise_pair(P, F.fid, g.kxp, pos, 0, lo, hi);
+              if (z3) noise_pair(P, nk, F.fid, g.kxp, g.lineky, pos, lo, hi);
+              else noise_pair(P, nk, F.fid, g.kxp, pos, 0, lo, hi);
               xi[i] = lo;
               if (L > 1) xi[i + HALF] = hi;
             }
@@ -203,7 +209,7 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
           float2 xi = make_float2(0.f, 0.f);
           if (F.noisy) {
             const int pos = pos_step2<L>(m, i);
-            xi = z3 ? noise_at(P, F.fid, g.kxp, g.lineky, pos) : noise_at(P, F.fid, g.kxp, pos, 0);
+            xi = z3 ? noise_at(P, nk, F.fid, g.kxp, g.lineky, pos) : noise_at(P, nk, F.fid, g.kxp, pos, 0);
           }
           update_mode<L, Prog>(P, F, fi, g, i, z3, smem, slot_sz, Cs, has_chan, xi);
         }
@@ -227,15 +233,15 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
         fx.states = P.state;
         fx.srcs = F.src;
         fx.es = g.elem(pos);
-        if (z3) fx.ep = (size_t)((sy - ky) & (sy - 1)) * P.Lx + (size_t)ppos * g.pstride;
+        if (z3) fx.ep = g.mbase + (size_t)((sy - ky) & (sy - 1)) * P.Lx + (size_t)ppos * g.pstride;
         else fx.ep = g.elem(ppos);
         fx.wsel = 0;
         const VPoint v0 = make_vpoint(P, 0, ky, kz);
-        fx.xi = F.noisy ? noise_at(P, F.fid, 0, ky, kz) : make_float2(0.f, 0.f);
+        fx.xi = F.noisy ? noise_at(P, nk, F.fid, 0, ky, kz) : make_float2(0.f, 0.f);
         const float2 o0 = Prog::eval(P, fi, v0, fx);
         fx.wsel = 1;
         const VPoint v1 = make_vpoint(P, P.sx / 2, ky, kz);
-        fx.xi = F.noisy ? noise_at(P, F.fid, P.sx / 2, ky, kz) : make_float2(0.f, 0.f);
+        fx.xi = F.noisy ? noise_at(P, nk, F.fid, P.sx / 2, ky, kz) : make_float2(0.f, 0.f);
         const float2 o1 = Prog::eval(P, fi, v1, fx);
         const float2 z = c_add(o0, c_muli(o1));
         const float2 a = (has_chan && keep_point(P, v0, F)) ? c_scale(o0, P.invN) : make_float2(0.f, 0.f);

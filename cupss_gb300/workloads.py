@@ -26,3 +26,39 @@ def splitmix64_uniform(n, seed=DEFAULT_SEED, lo=-0.1, hi=0.1):
 # 05_edwards_wilkinson, 06_kpz of the reference).
 CH_EQ = "dt phi + q^2*(a + k*q^2)*phi = -b*q^2*phi^3"
 CH_NOISE = "2*T*q^2"
+
+# Systems of the batched and served workloads, as evolver declarations.
+SYSTEMS = {
+    "kpz": dict(fields=[("h", True), ("iqxh", False), ("iqyh", False)],
+                params={"nu": 1.0, "lam": 1.0, "D": 1.0},
+                eqs=["dt h + nu*q^2*h = 0.5*lam*iqxh^2 + 0.5*lam*iqyh^2", "iqxh = iqx*h", "iqyh = iqy*h"],
+                noise=[("h", "2*D")], out="h"),
+    "ew": dict(fields=[("h", True)], params={"nu": 1.0, "D": 1.0}, eqs=["dt h + nu*q^2*h = 0"],
+               noise=[("h", "2*D")], out="h"),
+    "ch": dict(fields=[("phi", True)], params={"a": -1.0, "b": 1.0, "k": 1.0, "T": 0.01},
+               eqs=[CH_EQ], noise=[("phi", CH_NOISE)], out="phi"),
+}
+
+
+def declare(target, system):
+    """Declares a SYSTEMS entry on an Evolver or Ensemble (same method names)."""
+    for nm, dyn in system["fields"]:
+        target.createField(nm, dyn)
+    for k, v in system["params"].items():
+        target.addParameter(k, v)
+    for q in system["eqs"]:
+        target.addEquation(q)
+    for f, a in system["noise"]:
+        target.addNoise(f, a)
+
+
+def kpz_ensemble(n=512, seed=DEFAULT_SEED, sizes=(64, 128, 256, 512)):
+    """Members of the KPZ ensemble: square 2D grids drawn uniformly from `sizes` (log-
+    uniform in N), nu ~ U[0.5, 2], lambda ~ U[0, 4], D = 1, own Philox seed each, h0 = 0.
+    Returns a list of dicts (n_side, nu, lam, seed)."""
+    rng = np.random.default_rng(seed)
+    side = rng.choice(np.asarray(sizes), size=n)
+    nu = rng.uniform(0.5, 2.0, size=n)
+    lam = rng.uniform(0.0, 4.0, size=n)
+    return [dict(side=int(side[i]), nu=float(nu[i]), lam=float(lam[i]), seed=int(seed) * 4096 + i)
+            for i in range(n)]

@@ -148,6 +148,38 @@ int cupssgb_solver_set_generated_programs(cupssgb_solver* s, int on);
  * Returns the cubin size (> 0) or CUPSSGB_ERR_CUDA with the NVRTC log in `log`. */
 int cupssgb_jit_check(const char* source, char* log, int loglen);
 
+/* ---------------- batches ----------------
+ * No counterpart in the reference (one system per evolver).  set_members(n) before
+ * prepare turns a solver into a batch of n independent systems with the solver's
+ * structure and grid: same fields, terms and q-monomials; each member has its own
+ * prefactor values, noise amplitude, seed, state and step count.  advance() then
+ * steps every active member in the same launches (replayed from CUDA graphs), and a
+ * member's trajectory is the one a single solver with its values and seed gives.
+ * The turnaround tile width is autotuned at prepare (tune_report).  Member m's
+ * default seed is the solver's seed + m.  Member calls on a single solver: member 0. */
+int cupssgb_solver_set_members(cupssgb_solver* s, int n);
+int cupssgb_solver_members(const cupssgb_solver* s);
+/* Values for member m; the q-monomials (exponents) must equal the solver's. */
+int cupssgb_solver_set_member_term_pres(cupssgb_solver* s, int member, int field, int term, const cupssgb_pres* pres,
+                                        int n);
+int cupssgb_solver_set_member_implicit(cupssgb_solver* s, int member, int field, const cupssgb_pres* pres, int n);
+int cupssgb_solver_set_member_noise(cupssgb_solver* s, int member, int field, const cupssgb_pres* amp);
+int cupssgb_solver_set_member_seed(cupssgb_solver* s, int member, unsigned long long seed);
+/* Inactive members are skipped by every launch and count no steps (slot reuse). */
+int cupssgb_solver_set_member_active(cupssgb_solver* s, int member, int active);
+/* Zeroes member m's fields and dealiased copies and its step count (a fresh solve). */
+int cupssgb_solver_reset_member(cupssgb_solver* s, int member);
+/* Steps member m has taken (synchronises the solver's stream); negative on error. */
+long long cupssgb_solver_member_step(cupssgb_solver* s, int member);
+/* set_real / get_real of member m (host: synchronous; device: stream-ordered). */
+int cupssgb_solver_set_real_member(cupssgb_solver* s, int field, int member, const float* host_real);
+int cupssgb_solver_set_real_member_device(cupssgb_solver* s, int field, int member, const float* dev_real);
+int cupssgb_solver_get_real_member(cupssgb_solver* s, int field, int member, float* host_real);
+int cupssgb_solver_get_real_member_device(cupssgb_solver* s, int field, int member, float* dev_real);
+/* JSON {"phaseN": {"W": chosen, "ms": {candidate: ms per phase}}}; same buffer rules
+ * as kernel_report. */
+int cupssgb_solver_tune_report(cupssgb_solver* s, char* buf, int buflen);
+
 /* ---------------- process helpers ---------------- */
 /* Page-locked host memory for the host-buffer entry points (cudaMallocHost). */
 int cupssgb_host_alloc(long long bytes, void** out);
@@ -220,6 +252,31 @@ cupssgb_solver* cupssgb_evolver_solver(cupssgb_evolver* e);
  * with_cuda = 0.  fn = NULL removes it. */
 typedef void (*cupssgb_callback)(void* evolver, float* field_pairs, int sx, int sy, int sz);
 int cupssgb_evolver_set_callback(cupssgb_evolver* e, const char* field, int fourier, cupssgb_callback fn);
+
+/* ---------------- ensemble level ----------------
+ * The C++ class `ensemble` (include/cupss/ensemble.h) flattened to C: one system
+ * declared with the evolver's calls, many members that differ in grid, time step,
+ * seed and parameter values, grouped into batch solvers at prepare.  add_member
+ * returns the member index.  advance runs every member nsteps and returns when all
+ * are done.  describe: JSON list of the groups (grid, dt, members, autotuning). */
+typedef struct cupssgb_ensemble cupssgb_ensemble;
+int cupssgb_ensemble_create(cupssgb_ensemble** out);
+int cupssgb_ensemble_destroy(cupssgb_ensemble* e);
+int cupssgb_ensemble_create_field(cupssgb_ensemble* e, const char* name, int dynamic);
+int cupssgb_ensemble_add_parameter(cupssgb_ensemble* e, const char* name, float value);
+int cupssgb_ensemble_add_equation(cupssgb_ensemble* e, const char* equation);
+int cupssgb_ensemble_add_noise(cupssgb_ensemble* e, const char* field, const char* amplitude);
+int cupssgb_ensemble_add_member(cupssgb_ensemble* e, int sx, int sy, int sz, float dx, float dy, float dz, float dt,
+                                unsigned long long seed);
+int cupssgb_ensemble_set_member_parameter(cupssgb_ensemble* e, int member, const char* name, float value);
+int cupssgb_ensemble_prepare(cupssgb_ensemble* e);
+int cupssgb_ensemble_set_real(cupssgb_ensemble* e, int member, const char* field, const float* host_real);
+int cupssgb_ensemble_advance(cupssgb_ensemble* e, int nsteps);
+int cupssgb_ensemble_get_real(cupssgb_ensemble* e, int member, const char* field, float* host_real);
+int cupssgb_ensemble_groups(const cupssgb_ensemble* e);
+long long cupssgb_ensemble_device_bytes(const cupssgb_ensemble* e);
+long long cupssgb_ensemble_launch_count(const cupssgb_ensemble* e);
+int cupssgb_ensemble_describe(const cupssgb_ensemble* e, char* buf, int buflen);
 
 #ifdef __cplusplus
 }

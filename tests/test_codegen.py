@@ -39,3 +39,37 @@ def test_generated_programs_compile(built_lib, case, shape):
     for src in srcs:
         assert "cupssgb_turn" in src
         assert jit_check(src) > 0
+
+
+@pytest.mark.parametrize("case", range(len(CORPUS)))
+def test_batched_programs_compile(built_lib, case):
+    """The batch variant (values from the member's row of the value table) compiles too."""
+    from cupss_gb300.api import jit_check
+    from tests.test_parser_parity import build_lib
+    ir = build_lib(*CORPUS[case])
+    s = solver_from_ir(ir, (32, 16, 1))
+    s.set_members(8)
+    for src in s.generated_sources():
+        assert "P.mvals" in src and "P.pres[" not in src
+        assert jit_check(src) > 0
+    s.close()
+
+
+def test_ensemble_declaration_errors(built_lib):
+    """Errors the ensemble reports before touching a GPU."""
+    import cupss_gb300 as c
+    e = c.Ensemble()
+    e.createField("h", True)
+    e.addParameter("nu", 1.0)
+    with pytest.raises(c.CupssError):
+        e.createField("h", False)
+    with pytest.raises(c.CupssError):
+        e.addNoise("nope", "1")
+    m = e.addMember(32, 32, 1, dt=0.01, seed=1)
+    with pytest.raises(c.CupssError):
+        e.setMemberParameter(m, "lam", 2.0)
+    e.addEquation("dt h + nu*q^2*h = bogus*h")
+    with pytest.raises(c.CupssError) as ex:
+        e.prepare()
+    assert ex.value.code == c.capi.ERR_PARSE
+    e.close()

@@ -368,6 +368,111 @@ def bench_ensemble(args):
     print(json.dumps(line), flush=True)
 
 
+def bench_served(args):
+    """Served Poisson stream (EW, KPZ, CH 2D, CH 3D requests of mixed grids and step
+    counts) through the continuous-batching server vs the same requests run one after
+    another with the plain evolver (a FIFO single-solve server with the same arrival
+    times).  Latency = completion - arrival.  Pools (batched) and update programs
+    (both paths) are compiled before the stream starts."""
+    import cupss_gb300 as c
+    from cupss_gb300 import build as b
+    from cupss_gb300.workloads import SYSTEMS, initial_fields, served_stream
+    b.build()
+    reqs = served_stream(args.requests, args.rate)
+    keys = sorted({(r["system"], r["shape"], r["dt"]) for r in reqs})
+    srv = c.Server(hbm_budget=args.hbm_budget, max_slots=args.max_slots, max_chunk=args.max_chunk)
+    sids = {k: srv.addSystem(SYSTEMS[k]) for k in ("ew", "kpz", "ch")}
+    t0 = time.perf_counter()
+    for sysname, shape, dt in keys:
+        srv.warm(sids[sysname], shape, dt)
+    warm_s = time.perf_counter() - t0
+
+    def plain_solve(r, steps=None):
+        sd = SYSTEMS[r["system"]]
+        e = c.Evolver(True, *r["shape"], dt=r["dt"], write_every=10 ** 9)
+        for nm, dyn in sd["fields"]:
+            e.createField(nm, dyn)
+        for k, v in sd["params"].items():
+            e.addParameter(k, r["params"].get(k, v))
+        for q in sd["eqs"]:
+            e.addEquation(q)
+        for f, a in sd["noise"]:
+            e.addNoise(f, a)
+        e.setNoiseSeed(r["seed"])
+        for nm, arr in initial_fields(r).items():
+            e.setReal(nm, arr)
+        e.prepareProblem()
+        e.advanceTime(steps or r["steps"])
+        out = e.getReal(sd["out"])
+        e.close()
+        return out
+
+    for sysname, shape, dt in keys:   # compile the plain path's programs
+        plain_solve(dict(system=sysname, shape=shape, dt=dt, params={}, seed=0, init_seed=0), steps=1)
+
+    clocks = Clocks(0)
+    clocks.start()
+    ids = []
+    start = time.perf_counter()
+    for r in reqs:
+        delay = start + r["arrival"] - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        ids.append(srv.submit(sids[r["system"]], r["shape"], r["dt"], r["steps"], seed=r["seed"],
+                              params=r["params"], init=initial_fields(r)))
+    for rid in ids:
+        srv.wait(rid)
+    clk = clocks.stop()
+    times = [srv.times(rid) for rid in ids]
+    t_first = min(t[0] for t in times)
+    makespan = max(t[2] for t in times) - t_first
+    lat = np.array([t[2] - t[0] for t in times])
+    served = [srv.result(rid) for rid in ids]
+    stats = srv.stats()
+    srv.close()
+
+    # plain: service time of each request alone, FIFO in arrival order
+    svc = []
+    agree = 0
+    for r, got in zip(reqs, served):
+        t1 = time.perf_counter()
+        ref = plain_solve(r)
+        svc.append(time.perf_counter() - t1)
+        fa, fb = bool(np.isfinite(ref).all()), bool(np.isfinite(got).all())
+        if fa and fb:
+            d = np.linalg.norm(got.astype(np.float64) - ref) / max(np.linalg.norm(ref), 1e-30)
+            agree += d < 1e-6
+        else:
+            agree += fa == fb
+    done, plat = 0.0, []
+    for r, s_i in zip(reqs, svc):
+        done = max(done, r["arrival"]) + s_i
+        plat.append(done - r["arrival"])
+    plat = np.array(plat)
+    work = float(sum(np.prod(r["shape"]) * r["steps"] for r in reqs))
+    line = {"metric": "served solves/s", "value": len(reqs) / makespan, "unit": "solves/s", "n_gpus": 1,
+            "steps": None, "warmup": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic Poisson stream, seed 20261203",
+            "config": {"workload": "served: %d requests, Poisson rate %.2f/s, {EW, KPZ, CH} 2D 64^2..1024^2, "
+                                   "CH 3D 64^3..128^3, steps log-U[1e3,1e5]" % (len(reqs), args.rate),
+                       "requests": len(reqs), "rate_per_s": args.rate, "hbm_budget": args.hbm_budget,
+                       "max_slots": args.max_slots, "max_chunk": args.max_chunk, "pool_keys": len(keys),
+                       "total_pt_steps": work},
+            "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                          "max": float(lat.max())},
+            "pt_steps_per_s": work / makespan, "makespan_s": makespan,
+            "plain_sequential": {"value": len(reqs) / (done - reqs[0]["arrival"]), "unit": "solves/s",
+                                 "latency_s": {"p50": float(np.percentile(plat, 50)),
+                                               "p99": float(np.percentile(plat, 99))},
+                                 "service_s_total": float(sum(svc)),
+                                 "what": "each request alone: evolver create + prepare + advance + getReal, "
+                                         "FIFO in arrival order (programs precompiled)"},
+            "speedup_vs_plain": (done - reqs[0]["arrival"]) / makespan,
+            "accuracy": {"requests_equal_to_plain": int(agree), "tolerance": "rel L2 1e-6"},
+            "server_stats": stats, "warm_s": warm_s, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -397,7 +502,12 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=None)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="ch3d-256", choices=sorted(WORKLOADS) + ["kpz-ensemble"])
+    ap.add_argument("--workload", default="ch3d-256", choices=sorted(WORKLOADS) + ["kpz-ensemble", "served"])
+    ap.add_argument("--requests", type=int, default=64)
+    ap.add_argument("--rate", type=float, default=2.0)
+    ap.add_argument("--hbm-budget", type=float, default=150e9)
+    ap.add_argument("--max-slots", type=int, default=32)
+    ap.add_argument("--max-chunk", type=int, default=256)
     ap.add_argument("--members", type=int, default=512)
     ap.add_argument("--plain-members", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -408,6 +518,8 @@ def main():
     args = ap.parse_args()
     if args.workload == "kpz-ensemble":
         return bench_ensemble(args)
+    if args.workload == "served":
+        return bench_served(args)
     wl = WORKLOADS[args.workload]
     K = args.steps if args.steps is not None else wl["steps"]
     W = args.warmup if args.warmup is not None else wl["warmup"]

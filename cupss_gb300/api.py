@@ -162,6 +162,9 @@ class Solver:
         capi.check(self.lib.cupssgb_solver_get_real_member(self.h, f, m, capi.fptr(out)))
         return out.reshape(self.shape)
 
+    def estimate_bytes(self, members=1):
+        return capi.check(self.lib.cupssgb_solver_estimate_bytes(self.h, int(members)))
+
     def tune_report(self):
         n = capi.check(self.lib.cupssgb_solver_tune_report(self.h, None, 0))
         buf = C.create_string_buffer(n + 1)
@@ -378,4 +381,97 @@ class Ensemble:
         n = capi.check(self.lib.cupssgb_ensemble_describe(self.h, None, 0))
         buf = C.create_string_buffer(n + 1)
         self.lib.cupssgb_ensemble_describe(self.h, buf, n + 1)
+        return json.loads(buf.value.decode())
+
+
+class Server:
+    """Mirror of the C++ ``server`` (include/cupss/server.h): continuous batching of
+    independent solves within an HBM budget, scheduled by a native thread."""
+
+    def __init__(self, hbm_budget=150e9, max_slots=32, max_chunk=256):
+        self.lib = capi.load()
+        h = C.c_void_p()
+        capi.check(self.lib.cupssgb_server_create(float(hbm_budget), int(max_slots), int(max_chunk), C.byref(h)))
+        self.h = h
+        self.shapes = {}
+
+    def close(self):
+        if self.h:
+            self.lib.cupssgb_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def addSystem(self, system=None):
+        """New system id; `system` (a workloads.SYSTEMS entry) declares it at once."""
+        sid = capi.check(self.lib.cupssgb_server_add_system(self.h))
+        if system is not None:
+            for nm, dyn in system["fields"]:
+                self.createField(sid, nm, dyn)
+            for k, v in system["params"].items():
+                self.addParameter(sid, k, v)
+            for q in system["eqs"]:
+                self.addEquation(sid, q)
+            for f, a in system["noise"]:
+                self.addNoise(sid, f, a)
+            if "out" in system:
+                self.setOutputField(sid, system["out"])
+        return sid
+
+    def createField(self, sid, name, dynamic):
+        return capi.check(self.lib.cupssgb_server_create_field(self.h, sid, name.encode(), int(bool(dynamic))))
+
+    def addParameter(self, sid, name, value):
+        return capi.check(self.lib.cupssgb_server_add_parameter(self.h, sid, name.encode(), float(value)))
+
+    def addEquation(self, sid, eq):
+        return capi.check(self.lib.cupssgb_server_add_equation(self.h, sid, eq.encode()))
+
+    def addNoise(self, sid, name, amp):
+        return capi.check(self.lib.cupssgb_server_add_noise(self.h, sid, name.encode(), amp.encode()))
+
+    def setOutputField(self, sid, name):
+        return capi.check(self.lib.cupssgb_server_set_output_field(self.h, sid, name.encode()))
+
+    def submit(self, sid, shape, dt, nsteps, seed=0, params=None, init=None, cell=(1.0, 1.0, 1.0)):
+        sx, sy, sz = shape
+        params = params or {}
+        init = init or {}
+        names = (C.c_char_p * max(len(params), 1))(*[k.encode() for k in params])
+        vals = (C.c_float * max(len(params), 1))(*[float(v) for v in params.values()])
+        arrays = [np.ascontiguousarray(np.asarray(a, np.float32).reshape(-1)) for a in init.values()]
+        for a in arrays:
+            assert a.size == sx * sy * sz
+        fields = (C.c_char_p * max(len(init), 1))(*[k.encode() for k in init])
+        ptrs = (capi._FP * max(len(init), 1))(*[capi.fptr(a) for a in arrays])
+        rid = capi.check(self.lib.cupssgb_server_submit(self.h, sid, sx, sy, sz, *cell, float(dt), int(nsteps),
+                                                        int(seed), len(params), names, vals, len(init), fields,
+                                                        ptrs))
+        self.shapes[rid] = (sz, sy, sx)
+        return rid
+
+    def warm(self, sid, shape, dt, cell=(1.0, 1.0, 1.0)):
+        return capi.check(self.lib.cupssgb_server_warm(self.h, sid, *shape, *cell, float(dt)))
+
+    def wait(self, rid, timeout=-1.0):
+        return bool(capi.check(self.lib.cupssgb_server_wait(self.h, rid, float(timeout))))
+
+    def result(self, rid):
+        out = np.empty(int(np.prod(self.shapes[rid])), np.float32)
+        capi.check(self.lib.cupssgb_server_result(self.h, rid, capi.fptr(out)))
+        return out.reshape(self.shapes[rid])
+
+    def times(self, rid):
+        t = (C.c_double * 3)()
+        capi.check(self.lib.cupssgb_server_times(self.h, rid, t))
+        return tuple(t)
+
+    def stats(self):
+        n = capi.check(self.lib.cupssgb_server_stats(self.h, None, 0))
+        buf = C.create_string_buffer(n + 1)
+        self.lib.cupssgb_server_stats(self.h, buf, n + 1)
         return json.loads(buf.value.decode())

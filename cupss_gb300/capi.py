@@ -97,6 +97,8 @@ SIGNATURES = {
     "cupssgb_solver_get_real_member": (_I, [_P, _I, _I, _FP]),
     "cupssgb_solver_get_real_member_device": (_I, [_P, _I, _I, _P]),
     "cupssgb_solver_tune_report": (_I, [_P, C.c_char_p, _I]),
+    "cupssgb_solver_estimate_bytes": (_LL, [_P, _I]),
+    "cupssgb_solver_query": (_I, [_P]),
     "cupssgb_real_to_fourier_noalloc": (_I, [_P, _P, _I, _I, _I, _P]),
     "cupssgb_host_alloc": (_I, [_LL, C.POINTER(_P)]),
     "cupssgb_host_free": (_I, [_P]),
@@ -137,6 +139,21 @@ SIGNATURES = {
     "cupssgb_ensemble_device_bytes": (_LL, [_P]),
     "cupssgb_ensemble_launch_count": (_LL, [_P]),
     "cupssgb_ensemble_describe": (_I, [_P, C.c_char_p, _I]),
+    "cupssgb_server_create": (_I, [C.c_double, _I, _I, C.POINTER(_P)]),
+    "cupssgb_server_destroy": (_I, [_P]),
+    "cupssgb_server_add_system": (_I, [_P]),
+    "cupssgb_server_create_field": (_I, [_P, _I, _S, _I]),
+    "cupssgb_server_add_parameter": (_I, [_P, _I, _S, _F]),
+    "cupssgb_server_add_equation": (_I, [_P, _I, _S]),
+    "cupssgb_server_add_noise": (_I, [_P, _I, _S, _S]),
+    "cupssgb_server_set_output_field": (_I, [_P, _I, _S]),
+    "cupssgb_server_submit": (_LL, [_P, _I, _I, _I, _I, _F, _F, _F, _F, _LL, _ULL, _I, C.POINTER(_S), _FP, _I,
+                                    C.POINTER(_S), C.POINTER(_FP)]),
+    "cupssgb_server_warm": (_I, [_P, _I, _I, _I, _I, _F, _F, _F, _F]),
+    "cupssgb_server_wait": (_I, [_P, _LL, C.c_double]),
+    "cupssgb_server_result": (_I, [_P, _LL, _FP]),
+    "cupssgb_server_times": (_I, [_P, _LL, C.POINTER(C.c_double)]),
+    "cupssgb_server_stats": (_I, [_P, C.c_char_p, _I]),
 }
 
 _lib = None

@@ -8,6 +8,7 @@
 
 #include "../../include/cupss.h"
 #include "../../include/cupss/ensemble.h"
+#include "../../include/cupss/server.h"
 #include "../../include/cupss_gb300.h"
 #include "engine.h"
 #include "host_common.h"
@@ -23,6 +24,10 @@ struct cupssgb_evolver {
 
 struct cupssgb_ensemble {
   ensemble* e;
+};
+
+struct cupssgb_server {
+  server* s;
 };
 
 namespace {
@@ -734,6 +739,21 @@ int cupssgb_solver_tune_report(cupssgb_solver* s, char* buf, int buflen) {
   return copy_out(r, buf, buflen);
 }
 
+long long cupssgb_solver_estimate_bytes(cupssgb_solver* s, int members) {
+  if (!s) return fail(CUPSSGB_ERR_INVALID, "null handle");
+  long long out = 0;
+  const int rc = guard([&] {
+    out = (long long)s->s->estimate_bytes(members);
+    return 0;
+  });
+  return rc != 0 ? rc : out;
+}
+
+int cupssgb_solver_query(cupssgb_solver* s) {
+  NEED(s);
+  return guard([&] { return s->s->idle() ? 1 : 0; });
+}
+
 /* ---------------- ensembles ---------------- */
 
 int cupssgb_ensemble_create(cupssgb_ensemble** out) {
@@ -828,6 +848,123 @@ int cupssgb_ensemble_describe(const cupssgb_ensemble* e, char* buf, int buflen) 
   std::string r;
   const int rc = guard([&] {
     r = e->e->describe();
+    return 0;
+  });
+  if (rc != 0) return rc;
+  return copy_out(r, buf, buflen);
+}
+
+/* ---------------- server ---------------- */
+
+int cupssgb_server_create(double hbm_budget, int max_slots, int max_chunk, cupssgb_server** out) {
+  NEED(out);
+  return guard([&] {
+    *out = new cupssgb_server{new server(hbm_budget, max_slots, max_chunk)};
+    return 0;
+  });
+}
+
+int cupssgb_server_destroy(cupssgb_server* s) {
+  if (!s) return 0;
+  return guard([&] {
+    delete s->s;
+    delete s;
+    return 0;
+  });
+}
+
+int cupssgb_server_add_system(cupssgb_server* s) {
+  NEED(s);
+  return guard([&] { return s->s->addSystem(); });
+}
+
+int cupssgb_server_create_field(cupssgb_server* s, int system, const char* name, int dynamic) {
+  NEED(s);
+  NEED(name);
+  return guard([&] { return s->s->createField(system, name, dynamic != 0); });
+}
+
+int cupssgb_server_add_parameter(cupssgb_server* s, int system, const char* name, float value) {
+  NEED(s);
+  NEED(name);
+  return guard([&] { return s->s->addParameter(system, name, value); });
+}
+
+int cupssgb_server_add_equation(cupssgb_server* s, int system, const char* equation) {
+  NEED(s);
+  NEED(equation);
+  return guard([&] { return s->s->addEquation(system, equation); });
+}
+
+int cupssgb_server_add_noise(cupssgb_server* s, int system, const char* field, const char* amplitude) {
+  NEED(s);
+  NEED(field);
+  NEED(amplitude);
+  return guard([&] { return s->s->addNoise(system, field, amplitude); });
+}
+
+int cupssgb_server_set_output_field(cupssgb_server* s, int system, const char* field) {
+  NEED(s);
+  NEED(field);
+  return guard([&] { return s->s->setOutputField(system, field); });
+}
+
+long long cupssgb_server_submit(cupssgb_server* s, int system, int sx, int sy, int sz, float dx, float dy, float dz,
+                                float dt, long long nsteps, unsigned long long seed, int nparams,
+                                const char* const* names, const float* values, int ninit,
+                                const char* const* fields, const float* const* arrays) {
+  if (!s) return fail(CUPSSGB_ERR_INVALID, "null handle");
+  if ((nparams > 0 && (!names || !values)) || (ninit > 0 && (!fields || !arrays)))
+    return fail(CUPSSGB_ERR_INVALID, "null parameter or field array");
+  long long id = 0;
+  const int rc = guard([&] {
+    std::map<std::string, float> params;
+    for (int i = 0; i < nparams; ++i) params[names[i]] = values[i];
+    std::map<std::string, const float*> init;
+    for (int i = 0; i < ninit; ++i) init[fields[i]] = arrays[i];
+    id = s->s->submit(system, sx, sy, sz, dx, dy, dz, dt, nsteps, seed, params, init);
+    return 0;
+  });
+  return rc != 0 ? rc : id;
+}
+
+int cupssgb_server_warm(cupssgb_server* s, int system, int sx, int sy, int sz, float dx, float dy, float dz,
+                        float dt) {
+  NEED(s);
+  return guard([&] {
+    s->s->warm(system, sx, sy, sz, dx, dy, dz, dt);
+    return 0;
+  });
+}
+
+int cupssgb_server_wait(cupssgb_server* s, long long id, double timeout) {
+  NEED(s);
+  return guard([&] { return s->s->wait(id, timeout) ? 1 : 0; });
+}
+
+int cupssgb_server_result(cupssgb_server* s, long long id, float* host_out) {
+  NEED(s);
+  NEED(host_out);
+  return guard([&] {
+    s->s->result(id, host_out);
+    return 0;
+  });
+}
+
+int cupssgb_server_times(cupssgb_server* s, long long id, double* times3) {
+  NEED(s);
+  NEED(times3);
+  return guard([&] {
+    s->s->times(id, times3, times3 + 1, times3 + 2);
+    return 0;
+  });
+}
+
+int cupssgb_server_stats(cupssgb_server* s, char* buf, int buflen) {
+  NEED(s);
+  std::string r;
+  const int rc = guard([&] {
+    r = s->s->stats();
     return 0;
   });
   if (rc != 0) return rc;

@@ -92,6 +92,9 @@ class Solver {
   void reset_member(int m);                   // zero states and copies, step count 0
   long long member_step(int m);
   std::string tune_report() const;            // JSON: autotuned launch shapes per phase
+  // Device bytes prepare() would allocate for a batch of `members` (no GPU needed).
+  size_t estimate_bytes(int members);
+  bool idle();                                // all queued work on the stream has finished
   static constexpr int kGraphSteps = 16;
   void get_real_pairs_device(int f, float2* dst);   // reference float2 layout (x, 0)
   // Materialisation points for callbacks (src/field.cpp:48-86), all device pointers in

@@ -180,6 +180,11 @@ void Solver::autotune() {
   check(cudaEventCreate(&a), "cudaEventCreate");
   check(cudaEventCreate(&b), "cudaEventCreate");
   const long long l0 = launches_;
+  // time with every slot active (a pool may be prepared with all slots free)
+  std::vector<MemberK> all = members_h_;
+  for (MemberK& k : all) k.active = 1u;
+  check(cudaMemcpyAsync(members_d_, all.data(), all.size() * sizeof(MemberK), cudaMemcpyHostToDevice, stream_),
+        "member upload");
   for (Phase& P : phases_) {
     P.tune_ms.clear();
     if (P.fields.empty()) continue;
@@ -216,8 +221,34 @@ void Solver::autotune() {
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   launches_ = l0;
+  check(cudaMemcpyAsync(members_d_, members_h_.data(), members_h_.size() * sizeof(MemberK), cudaMemcpyHostToDevice,
+                        stream_),
+        "member upload");
   zero_dynamic_buffers();
   check(cudaStreamSynchronize(stream_), "autotune");
+}
+
+size_t Solver::estimate_bytes(int members) {
+  if (members < 1) throw Error(kErrInvalid, "members >= 1");
+  if (!prepared_) build_plan();
+  const size_t half = (size_t)Lx_ * sy_ * sz_, arr = half * sizeof(float2) * (size_t)members;
+  size_t b = 2 * 2048 * sizeof(float2) + npoints() * sizeof(float) + half * sizeof(float2);   // tables, scratch
+  for (int f = 0; f < nfields(); ++f) {
+    b += 2 * arr;
+    if (alias_order_[f] > 1) b += (dim_ == 3 ? 2 : 1) * arr;
+  }
+  for (const Phase& P : phases_) b += P.products.size() * arr;
+  if (members > 1 || batch_) b += (size_t)members * (sizeof(MemberK) + 2 * kMemberVals * sizeof(float));
+  return b;
+}
+
+bool Solver::idle() {
+  if (!stream_) return true;
+  const cudaError_t e = cudaStreamQuery(stream_);
+  if (e == cudaSuccess) return true;
+  if (e == cudaErrorNotReady) return false;
+  check(e, "cudaStreamQuery");
+  return false;
 }
 
 std::string Solver::tune_report() const {

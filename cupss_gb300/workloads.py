@@ -62,3 +62,45 @@ def kpz_ensemble(n=512, seed=DEFAULT_SEED, sizes=(64, 128, 256, 512)):
     lam = rng.uniform(0.0, 4.0, size=n)
     return [dict(side=int(side[i]), nu=float(nu[i]), lam=float(lam[i]), seed=int(seed) * 4096 + i)
             for i in range(n)]
+
+
+def served_stream(n=64, rate=2.0, seed=DEFAULT_SEED):
+    """Poisson stream of solve requests drawn uniformly from {2D Edwards-Wilkinson, 2D
+    KPZ, 2D Cahn-Hilliard, 3D Cahn-Hilliard}: 2D sides uniform over {64..1024} (log-
+    uniform in N), 3D sides over {64, 128} (the powers of two in 64..192), step counts
+    log-uniform in [1e3, 1e5], seeded parameters (nu ~ U[0.5, 2], KPZ lambda ~ U[0, 1],
+    CH T ~ U[0, 0.01]) and seeded initial fields (CH: U[-0.1, 0.1]; EW, KPZ: flat).
+    arrival: seconds after the first request."""
+    rng = np.random.default_rng(seed)
+    kinds = ["ew", "kpz", "ch2d", "ch3d"]
+    gaps = rng.exponential(1.0 / rate, size=n)
+    gaps[0] = 0.0
+    arrival = np.cumsum(gaps)
+    out = []
+    for i in range(n):
+        kind = kinds[int(rng.integers(4))]
+        steps = int(round(10.0 ** rng.uniform(3.0, 5.0)))
+        if kind == "ch3d":
+            side = int(rng.choice([64, 128]))
+            shape = (side, side, side)
+        else:
+            side = int(rng.choice([64, 128, 256, 512, 1024]))
+            shape = (side, side, 1)
+        if kind == "ew":
+            params, dt = {"nu": float(rng.uniform(0.5, 2.0))}, 0.01
+        elif kind == "kpz":
+            params, dt = {"nu": float(rng.uniform(0.5, 2.0)), "lam": float(rng.uniform(0.0, 1.0))}, 0.005
+        else:
+            params, dt = {"T": float(rng.uniform(0.0, 0.01))}, (0.01 if kind == "ch2d" else 0.005)
+        out.append(dict(kind=kind, system="ch" if kind.startswith("ch") else kind, shape=shape, dt=dt,
+                        steps=steps, params=params, seed=int(seed) * 8192 + i, init_seed=int(seed) + 17 * i,
+                        arrival=float(arrival[i])))
+    return out
+
+
+def initial_fields(req):
+    """Initial fields of a served_stream request (output field only; others start at 0)."""
+    if req["system"] != "ch":
+        return {}
+    n = int(np.prod(req["shape"]))
+    return {"phi": splitmix64_uniform(n, req["init_seed"], -0.1, 0.1).reshape(req["shape"][::-1])}

@@ -179,6 +179,10 @@ int cupssgb_solver_get_real_member_device(cupssgb_solver* s, int field, int memb
 /* JSON {"phaseN": {"W": chosen, "ms": {candidate: ms per phase}}}; same buffer rules
  * as kernel_report. */
 int cupssgb_solver_tune_report(cupssgb_solver* s, char* buf, int buflen);
+/* Device bytes prepare would allocate for a batch of `members` (no GPU needed). */
+long long cupssgb_solver_estimate_bytes(cupssgb_solver* s, int members);
+/* 1 when all work queued on the solver's stream has finished, 0 while it runs. */
+int cupssgb_solver_query(cupssgb_solver* s);
 
 /* ---------------- process helpers ---------------- */
 /* Page-locked host memory for the host-buffer entry points (cudaMallocHost). */
@@ -277,6 +281,37 @@ int cupssgb_ensemble_groups(const cupssgb_ensemble* e);
 long long cupssgb_ensemble_device_bytes(const cupssgb_ensemble* e);
 long long cupssgb_ensemble_launch_count(const cupssgb_ensemble* e);
 int cupssgb_ensemble_describe(const cupssgb_ensemble* e, char* buf, int buflen);
+
+/* ---------------- server level ----------------
+ * The C++ class `server` (include/cupss/server.h) flattened to C: a scheduler thread
+ * that admits submitted solves into batch-solver slots within an HBM budget, steps
+ * them with continuous batching and keeps finished results in host memory.
+ * Systems are declared once per add_system id.  submit copies the parameter values
+ * (names[i] = values[i]) and initial fields (fields[i] -> arrays[i], sx*sy*sz floats)
+ * and returns the request id (> 0).  wait returns 1 when done, 0 on timeout (timeout
+ * < 0: no limit).  result: the system's output field (set_output_field, default the
+ * first field).  times: seconds since the server started at submit, admission and
+ * completion.  warm: creates the pool for a system, grid and time step ahead of time
+ * (compilation and autotuning happen there, not in the first request). */
+typedef struct cupssgb_server cupssgb_server;
+int cupssgb_server_create(double hbm_budget, int max_slots, int max_chunk, cupssgb_server** out);
+int cupssgb_server_destroy(cupssgb_server* s);
+int cupssgb_server_add_system(cupssgb_server* s);
+int cupssgb_server_create_field(cupssgb_server* s, int system, const char* name, int dynamic);
+int cupssgb_server_add_parameter(cupssgb_server* s, int system, const char* name, float value);
+int cupssgb_server_add_equation(cupssgb_server* s, int system, const char* equation);
+int cupssgb_server_add_noise(cupssgb_server* s, int system, const char* field, const char* amplitude);
+int cupssgb_server_set_output_field(cupssgb_server* s, int system, const char* field);
+long long cupssgb_server_submit(cupssgb_server* s, int system, int sx, int sy, int sz, float dx, float dy, float dz,
+                                float dt, long long nsteps, unsigned long long seed, int nparams,
+                                const char* const* names, const float* values, int ninit,
+                                const char* const* fields, const float* const* arrays);
+int cupssgb_server_warm(cupssgb_server* s, int system, int sx, int sy, int sz, float dx, float dy, float dz,
+                        float dt);
+int cupssgb_server_wait(cupssgb_server* s, long long id, double timeout);
+int cupssgb_server_result(cupssgb_server* s, long long id, float* host_out);
+int cupssgb_server_times(cupssgb_server* s, long long id, double* times3);
+int cupssgb_server_stats(cupssgb_server* s, char* buf, int buflen);
 
 #ifdef __cplusplus
 }

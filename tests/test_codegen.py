@@ -73,3 +73,22 @@ def test_ensemble_declaration_errors(built_lib):
         e.prepare()
     assert ex.value.code == c.capi.ERR_PARSE
     e.close()
+
+
+def test_server_declaration_errors(built_lib):
+    """Errors the server reports on the caller's thread, before any GPU work."""
+    import cupss_gb300 as c
+    from cupss_gb300.workloads import SYSTEMS
+    srv = c.Server(hbm_budget=1e9)
+    sid = srv.addSystem(SYSTEMS["ew"])
+    with pytest.raises(c.CupssError):
+        srv.createField(sid, "h", True)
+    with pytest.raises(c.CupssError):
+        srv.setOutputField(sid, "nope")
+    with pytest.raises(c.CupssError):
+        srv.submit(sid, (32, 32, 1), 0.01, 10, params={"lam": 1.0})
+    with pytest.raises(c.CupssError):
+        srv.submit(sid + 5, (32, 32, 1), 0.01, 10)
+    with pytest.raises(c.CupssError):
+        srv.submit(sid, (32, 32, 1), 0.01, 0)
+    srv.close()

@@ -116,6 +116,17 @@ void Solver::set_noise(int f, bool on, const HostPres& amp) {
   invalidate_graphs();
 }
 
+void Solver::set_seed(uint64_t s) {
+  seed_ = s;
+  if (batch_) return;   // batch members keep their own seeds
+  members_h_.assign(1, MemberK{(uint32_t)(s & 0xffffffffu), (uint32_t)(s >> 32), 0u, 1u});
+  if (prepared_) {
+    check(cudaMemcpyAsync(members_d_, members_h_.data(), 2 * sizeof(uint32_t), cudaMemcpyHostToDevice, stream_),
+          "seed upload");
+    check(cudaStreamSynchronize(stream_), "seed upload");
+  }
+}
+
 void Solver::set_dt(float dt) {
   dt_ = dt;
   invalidate_graphs();
@@ -215,13 +226,15 @@ void Solver::prepare() {
       P.prodbuf.push_back((float2*)dalloc(hall * sizeof(float2)));
   scratch_real_ = (float*)dalloc(npoints() * sizeof(float));
   scratch_spec_ = (float2*)dalloc(half * sizeof(float2));
-  if (batch_) {
-    members_d_ = (MemberK*)dalloc((size_t)nmem_ * sizeof(MemberK));
+  // key, step count and active flag of each member (one for a single system)
+  if (!batch_)
+    members_h_.assign(1, MemberK{(uint32_t)(seed_ & 0xffffffffu), (uint32_t)(seed_ >> 32), 0u, 1u});
+  members_d_ = (MemberK*)dalloc((size_t)nmem_ * sizeof(MemberK));
+  check(cudaMemcpyAsync(members_d_, members_h_.data(), (size_t)nmem_ * sizeof(MemberK), cudaMemcpyHostToDevice,
+                        stream_),
+        "member upload");
+  if (batch_)
     for (int ph = 0; ph < 2; ++ph) mvals_d_[ph] = (float*)dalloc((size_t)nmem_ * kMemberVals * sizeof(float));
-    check(cudaMemcpyAsync(members_d_, members_h_.data(), (size_t)nmem_ * sizeof(MemberK), cudaMemcpyHostToDevice,
-                          stream_),
-          "member upload");
-  }
   check(cudaStreamSynchronize(stream_), "prepare sync");
   prepared_ = true;
   if (batch_) upload_member_values();
@@ -238,7 +251,7 @@ void Solver::prepare() {
       jit_kernel(turn_source(P, p, L, nl), "cupssgb_turn");
     }
   }
-  if (batch_) autotune();
+  autotune();
 }
 
 int Solver::pick_w(int L, int nl, int nslots) const {
@@ -478,7 +491,11 @@ void Solver::advance_phase(int phase) {
   if (phase < 0 || phase > 1) throw Error(kErrInvalid, "phase is 0 (non-dynamic) or 1 (dynamic)");
   if (batch_) throw Error(kErrUnsupported, "phase-wise stepping (callbacks) is for single systems");
   run_phase(phases_[phase]);
-  if (phase == 1) ++step_;
+  if (phase == 1) {
+    check(launch_tick(members_d_, nmem_, 1u, stream_), "member step count");
+    ++launches_;
+    ++step_;
+  }
 }
 
 void Solver::get_fourier(int f, float2* dst, bool on_device, int m) {
@@ -681,10 +698,8 @@ void Solver::run_phase(Phase& P) {
       }
     }
     x.tw = tw_;
-    if (batch_) {
-      x.mstride = half_;
-      x.members = members_d_;
-    }
+    x.members = members_d_;
+    if (batch_) x.mstride = half_;
     mark_begin();
     check(launch_row_pass(x, stream_, batch_ ? nmem_ : 1), "row pass");
     mark_end("row_pass");
@@ -707,10 +722,11 @@ void Solver::run_phase(Phase& P) {
   fill_turn(P, p, nslots, any_chan);
   p.W = pick_w(L, nl, nslots);
   if (turn_w_ > 0 && turn_w_ < p.W) p.W = turn_w_;
+  if (P.tuned_w > 0) p.W = P.tuned_w;
+  p.members = members_d_;
+  p.step_off = step_off_;
   if (batch_) {
-    if (P.tuned_w > 0) p.W = P.tuned_w;
     p.mstride = half_;
-    p.members = members_d_;
     p.mvals = mvals_d_[P.id];
   }
   dim3 grid((Lx_ + p.W - 1) / p.W, dim_ == 3 ? std::max(sy_ / 2, 1) : 1, batch_ ? nmem_ : 1);
@@ -817,11 +833,14 @@ double Solver::time_advance(int nsteps) {
   return ms;
 }
 
-void Solver::step_once() {
+// One time step; its noise uses step count + off.  tick: advance the device step counts.
+void Solver::step_once(uint32_t off, bool tick) {
+  step_off_ = off;
   run_phase(phases_[0]);
   run_phase(phases_[1]);
-  if (batch_) {
-    check(launch_tick(members_d_, nmem_, stream_), "member step count");
+  step_off_ = 0;
+  if (tick) {
+    check(launch_tick(members_d_, nmem_, off + 1u, stream_), "member step count");
     ++launches_;
   }
   ++step_;
@@ -829,12 +848,10 @@ void Solver::step_once() {
 
 void Solver::advance(int nsteps) {
   if (!prepared_) throw Error(kErrState, "advance before prepare");
-  if (batch_) {
-    if (mvals_dirty_) upload_member_values();
-    if (!timing_)
-      for (; nsteps >= kGraphSteps; nsteps -= kGraphSteps) run_graph();
-  }
-  for (int s = 0; s < nsteps; ++s) step_once();
+  if (batch_ && mvals_dirty_) upload_member_values();
+  if (!timing_)
+    for (; nsteps >= kGraphSteps; nsteps -= kGraphSteps) run_graph();
+  for (int s = 0; s < nsteps; ++s) step_once(0, true);
 }
 
 }  // namespace cupssgb

@@ -63,7 +63,7 @@ class Solver {
   int add_term(int f, const std::vector<int>& product, const std::vector<HostPres>& p);
   void set_term_pres(int f, int t, const std::vector<HostPres>& p);
   void set_noise(int f, bool on, const HostPres& amp);
-  void set_seed(uint64_t s) { seed_ = s; }
+  void set_seed(uint64_t s);
   void set_dt(float dt);
 
   void prepare();
@@ -80,7 +80,7 @@ class Solver {
   // then get its own prefactor values (same monomials), noise amplitude and seed.  Every
   // step launch covers all members (blockIdx.z = member); a member's noise counter is
   // its own step count, so its trajectory does not depend on the rest of the batch.
-  // Steps are replayed from CUDA graphs of kGraphSteps steps.
+  // Steps are replayed from CUDA graphs of kGraphSteps steps (single systems too).
   void set_members(int n);
   int members() const { return nmem_; }
   bool batched() const { return batch_; }
@@ -154,7 +154,7 @@ class Solver {
   int pick_w(int L, int nl, int nslots) const;
   void line_fwd_inv(int geo, int mode, const float2* in, float2* out, int xlimit, bool batch = false);
   void to_real_scratch(int f, int m);
-  void step_once();
+  void step_once(uint32_t off, bool tick);
   // batches
   void check_member(int m) const;
   void check_same_monomials(const std::vector<HostPres>& a, const std::vector<HostPres>& b) const;
@@ -192,6 +192,7 @@ class Solver {
   MemberK* members_d_ = nullptr;
   float* mvals_d_[2] = {nullptr, nullptr};
   bool mvals_dirty_ = false;
+  uint32_t step_off_ = 0;                        // step offset of the launches being issued
   cudaGraphExec_t graph_[2] = {nullptr, nullptr};   // by parity of the step count
   long long graph_launches_ = 0;                     // kernels per graph replay
 

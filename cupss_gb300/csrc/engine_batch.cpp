@@ -169,10 +169,11 @@ void Solver::zero_dynamic_buffers() {
   std::fill(par_.begin(), par_.end(), 0);
 }
 
-// Times each candidate tile width of every phase's turnaround on the batch itself
+// Times each candidate tile width of every phase's turnaround on the solver itself
 // (one warm-up and three timed runs of the whole phase) and keeps the fastest.  The
 // phases run on the zeroed buffers of a freshly prepared solver; every buffer is
-// zeroed again afterwards and no member step is counted.
+// zeroed again afterwards and no step is counted.  Runs for single systems too: a 2D
+// grid has only Lx/W turnaround CTAs, so narrow tiles can win on large 2D grids.
 void Solver::autotune() {
   const int L = (dim_ == 3) ? sz_ : sy_;
   const int nl = (dim_ == 3) ? 2 : 1;
@@ -198,7 +199,8 @@ void Solver::autotune() {
       continue;
     }
     std::vector<int> cands;
-    for (int w = wmax; w >= 1 && cands.size() < 3; w /= 2) cands.push_back(w);
+    for (int w = wmax; w >= 2 && cands.size() < 4; w /= 2) cands.push_back(w);
+    if (cands.empty()) cands.push_back(wmax);
     double best = 1e30;
     int best_w = wmax;
     for (int w : cands) {
@@ -286,7 +288,8 @@ void Solver::run_graph() {
     cudaGraph_t g = nullptr;
     check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
     try {
-      for (int s = 0; s < kGraphSteps; ++s) step_once();
+      // the launches of step s use step count + s; one counter update ends the graph
+      for (int s = 0; s < kGraphSteps; ++s) step_once((uint32_t)s, s == kGraphSteps - 1);
     } catch (...) {
       cudaStreamEndCapture(stream_, &g);
       if (g) cudaGraphDestroy(g);

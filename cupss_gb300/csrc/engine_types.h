@@ -99,11 +99,13 @@ struct LineParams {
   const float2* state[kMaxFields];  // current state of every field
   uint32_t key0, key1, step;
   const float2* tw;
-  // batches: member z's arrays start z * mstride elements after every pointer above;
-  // members / mvals are null for a single system (key, step and values above)
+  // members[z]: key, step count and active flag of the system at blockIdx.z (null: key and
+  // step above).  Batches: member z's arrays start z * mstride elements after every
+  // pointer above and its values are mvals[z] (null for a single system: values above).
   size_t mstride;
   const MemberK* members;
   const float* mvals;               // [member][kMemberVals]
+  uint32_t step_off;                // noise step = members[z].step + step_off (steps replayed in one graph)
 };
 
 enum XInMode : int { kXInSpectral = 0, kXInReal = 1, kXInRealPair = 2 };   // RealPair: float2 (x, y) reads .x

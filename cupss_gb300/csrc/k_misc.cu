@@ -107,13 +107,13 @@ __global__ void mask_spectrum(const MaskParams p) {
   }
 }
 
-__global__ void tick_members(MemberK* m, int n) {
+__global__ void tick_members(MemberK* m, int n, uint32_t inc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n && m[i].active) m[i].step += 1u;
+  if (i < n && m[i].active) m[i].step += inc;
 }
 
-cudaError_t launch_tick(MemberK* members, int n, cudaStream_t st) {
-  tick_members<<<(n + 255) / 256, 256, 0, st>>>(members, n);
+cudaError_t launch_tick(MemberK* members, int n, uint32_t inc, cudaStream_t st) {
+  tick_members<<<(n + 255) / 256, 256, 0, st>>>(members, n, inc);
   return cudaGetLastError();
 }
 

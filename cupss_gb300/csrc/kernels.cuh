@@ -103,12 +103,20 @@ row_pass(const XParams p) {
       continue;
     }
     const float2* in = p.in[c] + rowoff;
+    // the row goes through the transpose buffer once so that the mirrored element
+    // X[Lx - k] of the C2R pre-processing comes from shared memory
+    if (c > 0) __syncthreads();   // CTA-uniform: the previous channel's last reads of T
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       const int k = pos_step2<LX>(m, i);
-      float2 a = live ? in[k] : make_float2(0.f, 0.f);
-      float2 b = live ? in[(LX - k) & (LX - 1)] : make_float2(0.f, 0.f);
-      v[i] = c2r_pre(a, b, k, sx, p.tw);
+      v[i] = live ? in[k] : make_float2(0.f, 0.f);
+      T[pad_pos<LX>(k)] = v[i];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int k = pos_step2<LX>(m, i);
+      v[i] = c2r_pre(v[i], T[pad_pos<LX>((LX - k) & (LX - 1))], k, sx, p.tw);
     }
     inv_step2<LX>(v);
     __syncthreads();
@@ -189,8 +197,8 @@ line_pass(const LineParams P) {
   for (int c = 0; c < P.n_prod; ++c) {
     if (P.mode == kModeInv && g.kx0 > P.inv_xlimit[c]) continue;   // CTA-uniform
     float2* T = smem;
-    const float2* in = P.prod_in[c];
-    float2* out = P.prod_out[c];
+    const float2* in = g.at(P.prod_in[c]);
+    float2* out = g.at(P.prod_out[c]);
     if (P.mode == kModeFwd) {
 #pragma unroll
       for (int r = 0; r < R; ++r) v[r] = g.ok ? in[g.elem(pos_step1<L>(g.m, r))] : make_float2(0.f, 0.f);

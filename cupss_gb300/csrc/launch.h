@@ -18,8 +18,8 @@ int line_threads(int L, int nl, int W);
 cudaError_t launch_expand(const ExpandParams& p, cudaStream_t st);
 cudaError_t launch_compress(const CompressParams& p, cudaStream_t st);
 cudaError_t launch_mask(const MaskParams& p, cudaStream_t st);
-// Batches: advances the step count of every active member by one.
-cudaError_t launch_tick(MemberK* members, int n, cudaStream_t st);
+// Advances the step count of every active member by inc.
+cudaError_t launch_tick(MemberK* members, int n, uint32_t inc, cudaStream_t st);
 
 // per-L launchers (one translation unit per group of sizes)
 #define CUPSSGB_DECL_LINE(L) \

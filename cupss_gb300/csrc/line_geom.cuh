@@ -24,7 +24,8 @@ struct LineGeom {
   static constexpr int PL = padded_len<L>();
   int W, w, m, l, kx0, kxp, lineky;
   bool ok;
-  size_t lbase, pstride, slot_sz, mbase;
+  int lofs, pstride;     // element offset of this thread's line (position 0) and stride, within a member
+  size_t mbase, slot_sz;
   __device__ __forceinline__ explicit LineGeom(const LineParams& P) { init(P, blockIdx.x, blockIdx.y); }
   // Explicit tile coordinates (persistent kernels): tx = kx' tile, ty = line index.
   __device__ __forceinline__ LineGeom(const LineParams& P, int tx, int ty) { init(P, tx, ty); }
@@ -39,10 +40,10 @@ struct LineGeom {
     bool lineok = true;
     const int Lx = P.Lx;
     if (P.geo == kGeoCol) {
-      lbase = kxp;
+      lofs = kxp;
       pstride = Lx;
     } else if (P.geo == kGeoY3) {
-      lbase = (size_t)ty * P.sy * Lx + kxp;
+      lofs = ty * P.sy * Lx + kxp;
       pstride = Lx;
     } else {
       if (NL == 2) {
@@ -52,15 +53,19 @@ struct LineGeom {
       } else {
         lineky = ty;
       }
-      lbase = (size_t)lineky * Lx + kxp;
-      pstride = (size_t)P.sy * Lx;
+      lofs = lineky * Lx + kxp;
+      pstride = P.sy * Lx;
     }
     ok = (kxp < Lx) && lineok;
     mbase = (size_t)blockIdx.z * P.mstride;
-    lbase += mbase;
     slot_sz = (size_t)NL * PL * W;
   }
-  __device__ __forceinline__ size_t elem(int pos) const { return lbase + (size_t)pos * pstride; }
+  // 32-bit element index within the member; at(p) is p moved to this CTA's member.
+  __device__ __forceinline__ int elem(int pos) const { return lofs + pos * pstride; }
+  template <class T>
+  __device__ __forceinline__ T* at(T* p) const {
+    return p + mbase;
+  }
   __device__ __forceinline__ size_t sidx(int line, int pos) const {
     return (size_t)(line * PL + pad_pos<L>(pos)) * W + w;
   }

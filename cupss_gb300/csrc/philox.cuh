@@ -34,10 +34,12 @@ __device__ __forceinline__ void philox4x32_10(uint32_t& c0, uint32_t& c1, uint32
 // Box-Muller: two standard normals from two 32-bit words.
 //   u1 = ((a >> 8) + 1) 2^-24 in (0, 1],  u2 = (b >> 8) 2^-24 in [0, 1)
 //   r = sqrt(-2 ln u1),  theta = 2 pi (u2 - 1/2) in [-pi, pi)
+// ln and sin/cos use the hardware approximations (absolute error near 2^-21 on the
+// arguments here); the clamp keeps -2 ln u1 >= 0 where u1 rounds to 1.
 __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float& g1, float& g2) {
   const float u1 = (float)((a >> 8) + 1u) * 5.9604644775390625e-08f;
   const float u2 = (float)(b >> 8) * 5.9604644775390625e-08f;
-  const float r = sqrtf(-2.0f * logf(u1));
+  const float r = sqrtf(fmaxf(-2.0f * __logf(u1), 0.0f));
   float sn, cs;
   __sincosf(6.2831853071795864769f * (u2 - 0.5f), &sn, &cs);
   g1 = r * cs;

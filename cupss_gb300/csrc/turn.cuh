@@ -113,12 +113,12 @@ __device__ __forceinline__ void update_mode(const LineParams& P, const FieldK& F
   fx.src_direct = false;
   fx.states = P.state;
   fx.srcs = F.src;
-  fx.es = g.elem(pos);
+  fx.es = g.mbase + g.elem(pos);
   fx.ep = fx.es;
   fx.xi = xi;
   const VPoint vp = make_vpoint(P, g.kxp, z3 ? g.lineky : pos, z3 ? pos : 0);
   const float2 z = Prog::eval(P, fi, vp, fx);
-  F.next[g.elem(pos)] = z;
+  g.at(F.next)[g.elem(pos)] = z;
   if (has_chan) Cs[fx.as] = keep_point(P, vp, F) ? c_scale(z, P.invN) : make_float2(0.f, 0.f);
 }
 
@@ -130,7 +130,7 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
   if (P.members) {
     const MemberK mk = P.members[blockIdx.z];
     if (!mk.active) return;   // CTA-uniform, before any barrier
-    nk = NoiseKey{mk.key0, mk.key1, mk.step};
+    nk = NoiseKey{mk.key0, mk.key1, mk.step + P.step_off};
   }
   const LineGeom<L, NL> g(P);
   const int m = g.m, l = g.l;
@@ -142,7 +142,7 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
   // 1) forward transform of every product channel into its slot (step-2 positions)
   for (int c = 0; c < P.n_prod; ++c) {
     float2* Sl = smem + (size_t)c * slot_sz;
-    const float2* in = P.prod_in[c];
+    const float2* in = g.at(P.prod_in[c]);
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = g.ok ? in[g.elem(pos_step1<L>(m, r))] : make_float2(0.f, 0.f);
     fwd_step1<L>(v, m, P.tw);
@@ -165,7 +165,7 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
     //     the thread at once (generated programs load them directly, unrolled)
     for (int j = 0; j < F.nsrc; ++j) {
       float2* Sj = smem + (size_t)(P.n_prod + j) * slot_sz;
-      const float2* st = P.state[F.src[j]];
+      const float2* st = g.at(P.state[F.src[j]]);
 #pragma unroll
       for (int i = 0; i < R; ++i) {
         const int pos = pos_step2<L>(m, i);
@@ -232,9 +232,9 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
         fx.src_direct = false;
         fx.states = P.state;
         fx.srcs = F.src;
-        fx.es = g.elem(pos);
+        fx.es = g.mbase + g.elem(pos);
         if (z3) fx.ep = g.mbase + (size_t)((sy - ky) & (sy - 1)) * P.Lx + (size_t)ppos * g.pstride;
-        else fx.ep = g.elem(ppos);
+        else fx.ep = g.mbase + g.elem(ppos);
         fx.wsel = 0;
         const VPoint v0 = make_vpoint(P, 0, ky, kz);
         fx.xi = F.noisy ? noise_at(P, nk, F.fid, 0, ky, kz) : make_float2(0.f, 0.f);
@@ -246,7 +246,7 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
         const float2 z = c_add(o0, c_muli(o1));
         const float2 a = (has_chan && keep_point(P, v0, F)) ? c_scale(o0, P.invN) : make_float2(0.f, 0.f);
         const float2 b = (has_chan && keep_point(P, v1, F)) ? c_scale(o1, P.invN) : make_float2(0.f, 0.f);
-        F.next[g.elem(pos)] = z;
+        g.at(F.next)[g.elem(pos)] = z;
         if (has_chan) Cs[g.sidx(l, pos)] = c_add(a, c_muli(b));
       }
     }
@@ -271,7 +271,7 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
     inv_step1<L>(v, m, P.tw);
     if (g.ok) {
 #pragma unroll
-      for (int r = 0; r < R; ++r) F.chan[g.elem(pos_step1<L>(m, r))] = v[r];
+      for (int r = 0; r < R; ++r) g.at(F.chan)[g.elem(pos_step1<L>(m, r))] = v[r];
     }
     __syncthreads();   // Cs free for the next field
   }

@@ -612,7 +612,8 @@ def main():
     e2e = None
     if not args.no_e2e:
         # host-buffer path through the C-ABI: every step uploads the field from pinned
-        # host memory, advances one step and reads the field back
+        # host memory, advances one step and reads the field back into the other pinned
+        # buffer, which is the next step's input (the two buffers swap roles)
         pin_in = c.api.PinnedBuffer(N)
         pin_out = c.api.PinnedBuffer(N)
         pin_in.array[:] = init
@@ -623,12 +624,12 @@ def main():
             sv.set_real_ptr(0, pin_in.ptr)
             sv.advance(1)
             sv.get_real_ptr(0, pin_out.ptr)
-            pin_in.array[:] = pin_out.array
+            pin_in, pin_out = pin_out, pin_in
         el = reduce_max(time.perf_counter() - t0, ws)
         e2e = {"value": ws * N * args.e2e_steps / el, "unit": "pt-steps/s", "h2d_bytes_per_step": 4 * N,
                "d2h_bytes_per_step": 4 * N, "steps": args.e2e_steps,
                "path": "cupssgb_solver_set_real + cupssgb_solver_advance(1) + cupssgb_solver_get_real, "
-                       "pinned host buffers"}
+                       "two pinned host buffers alternating as input and output"}
         pin_in.close()
         pin_out.close()
         # a whole solve through the reference-facing evolver C-ABI, host in / host out

@@ -136,6 +136,7 @@ void Solver::set_dt(float dt) {
 void Solver::build_plan() {
   const int F = nfields();
   alias_order_.assign(F, 1);
+  chan_wide_.assign(F, 0);
   // term::prepareDevice (src/term_init.cpp:108-133): fields in products of size >= 2
   // are dealiased for the largest such product.
   for (const HostField& f : fields_)
@@ -481,7 +482,10 @@ void Solver::set_real_pairs_device(int f, const float2* real, const float2* deal
   forward_lines(st);
   if (alias_order_[f] > 1) {
     // the channel is the x spectrum scaled by 1/sx (see channel_from_state)
-    if (dealiased) row_pass_simple(kXInRealPair, dealiased, kXOutSpectral, chan_[f], 1.0f / (float)sx_);
+    if (dealiased) {
+      row_pass_simple(kXInRealPair, dealiased, kXOutSpectral, chan_[f], 1.0f / (float)sx_);
+      chan_wide_[f] = 1;
+    }
     else channel_from_state(f, chan_[f]);
   }
 }
@@ -629,11 +633,16 @@ void Solver::fill_turn(const Phase& P, LineParams& p, int& nslots, bool& any_cha
   int max_src = 0;
   for (int fi = 0; fi < p.nf; ++fi) max_src = std::max(max_src, p.f[fi].nsrc);
   p.src_slots = max_src;
-  nslots = p.n_prod + max_src + (any_chan ? 1 : 0);
+  // the inverse transform of the dealiased copies reuses slot 0 when the phase has one
+  // field; with several, it gets its own so the next field's states can stream in
+  const int data_slots = p.n_prod + max_src;
+  const bool own_tslot = any_chan && (p.nf > 1 || data_slots == 0);
+  p.tslot = own_tslot ? data_slots : 0;
+  nslots = data_slots + (own_tslot ? 1 : 0);
 }
 
 const std::string& Solver::turn_source(Phase& P, const LineParams& p, int L, int nl) {
-  std::vector<int> sig = {L, nl, p.nf, p.n_prod};
+  std::vector<int> sig = {L, nl, p.nf, p.n_prod, p.sx, p.sy, p.sz};
   for (int fi = 0; fi < p.nf; ++fi) {
     const FieldK& K = p.f[fi];
     sig.insert(sig.end(), {K.dynamic, K.noisy, K.nterms, K.term0, K.nimp, K.imp0, K.noise_q2n, K.noise_invq,
@@ -687,7 +696,12 @@ void Solver::run_phase(Phase& P) {
     x.out_mode = kXOutSpectral;
     x.out_scale = 1.f;
     x.n_in = (int)P.xin.size();
-    for (int i = 0; i < x.n_in; ++i) x.in[i] = chan_[P.xin[i]];
+    for (int i = 0; i < x.n_in; ++i) {
+      const int g = P.xin[i];
+      x.in[i] = chan_[g];
+      // columns beyond the dealias limit of the channel are zero: not read
+      x.in_xcols[i] = chan_wide_[g] ? 0 : std::min(Lx_, sx_ / (alias_order_[g] + 1) + 1);
+    }
     x.n_prod = (int)P.products.size();
     for (int q = 0; q < x.n_prod; ++q) {
       x.out[q] = P.prodbuf[q];

@@ -176,6 +176,9 @@ class Solver {
   uint64_t seed_ = 0x243F6A8885A308D3ull;
   std::vector<HostField> fields_;
   std::vector<int> alias_order_;
+  // chan_wide_[f]: the dealiased channel of f may hold content beyond its dealias limit
+  // (a real-space callback wrote it), so the row pass reads every column of it
+  std::vector<char> chan_wide_;
   bool prepared_ = false;
   bool use_jit_ = true;
   int turn_w_ = 0;            // 0: automatic tile width

@@ -87,6 +87,7 @@ struct LineParams {
   int geo, mode, W;
   float stepqx, stepqy, stepqz, dt, invN, sqrtN, sqrtHalfN;
   int src_slots;                    // turnaround: shared-memory slots for prefetched states
+  int tslot;                        // turnaround: transpose slot of the dealiased-copy inverse
   // products (turnaround) or channels to transform (fwd/inv passes)
   int n_prod;
   const float2* prod_in[kMaxProd];
@@ -117,6 +118,8 @@ struct XParams {
   float out_scale;                  // multiplies every product, in real or spectral output
   int n_in;
   const float2* in[kMaxXIn];        // spectral channels (float2) or real rows (as pairs)
+  int in_xcols[kMaxXIn];            // spectral inputs: columns kx' >= in_xcols are known zero
+                                    // and not read (0: every column is read)
   int n_prod;
   void* out[kMaxProd];
   int prod_n[kMaxProd];

@@ -123,9 +123,15 @@ struct LineCfg {
 
 // Twiddle super-table: the table for length L lives at tw + L and holds
 // exp(-2 pi i j / L) for j in [0, L).
+// The device load is a volatile read-only load: a kernel that runs a forward and an
+// inverse transform of the same length reads the same twiddles twice, and letting the
+// compiler merge those loads keeps every twiddle live in registers between the two
+// transforms (spills and lower occupancy); an L1 hit is cheaper than that.
 CG_HD float2 tw_load(const float2* tw, int L, int j) {
 #if defined(__CUDA_ARCH__)
-  return __ldg(tw + L + j);
+  float2 w;
+  asm volatile("ld.global.nc.v2.f32 {%0, %1}, [%2];" : "=f"(w.x), "=f"(w.y) : "l"(tw + L + j));
+  return w;
 #else
   return tw[L + j];
 #endif

@@ -141,10 +141,15 @@ std::string jit_generate_turn(const LineParams& p, int L, int NL, int min_blocks
     }
     o << "        return nv;\n      }\n";
   }
-  o << "    }\n    return make_float2(0.f, 0.f);\n  }\n};\n}  // namespace cupssgb\n"
+  o << "    }\n    return make_float2(0.f, 0.f);\n  }\n};\n"
+    // the phase structure and grid this kernel is specialised for
+    << "struct GenSpec {\n"
+    << "  static constexpr int kNF = " << p.nf << ";\n"
+    << "  static constexpr int kSX = " << p.sx << ", kSY = " << p.sy << ", kSZ = " << p.sz << ";\n"
+    << "};\n}  // namespace cupssgb\n"
     << "extern \"C\" __global__ void __launch_bounds__(256, " << min_blocks
     << ") cupssgb_turn(const cupssgb::LineParams P) {\n"
-    << "  cupssgb::turn_body<" << L << ", " << NL << ", cupssgb::GenProg>(P);\n}\n";
+    << "  cupssgb::turn_body<" << L << ", " << NL << ", cupssgb::GenProg, cupssgb::GenSpec>(P);\n}\n";
   return o.str();
 }
 

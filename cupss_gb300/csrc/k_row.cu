@@ -4,10 +4,29 @@
 
 namespace cupssgb {
 
+// One spectral input raised to one spectral product (phi^n): the register-resident form.
+static bool row_is_one(const XParams& p) {
+  return p.n_in == 1 && p.n_prod == 1 && p.in_mode == kXInSpectral && p.out_mode == kXOutSpectral &&
+         p.prod_n[0] >= 1 && p.prod_f[0][0] == 0;
+}
+
 template <int LX>
 static cudaError_t launch_row_t(const XParams& p, cudaStream_t st, int nz) {
   using C = RowCfg<LX>;
-  static bool attr = false;
+  static bool attr = false, attr_one = false;
+  dim3 block(C::M, C::RW);
+  dim3 grid((p.rows + C::RW - 1) / C::RW, 1, nz);
+  if (row_is_one(p)) {
+    const size_t smem = (size_t)C::RW * C::PL * sizeof(float2);
+    if (!attr_one) {
+      cudaError_t e = cudaFuncSetAttribute(row_pass_one<LX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           220 * 1024);
+      if (e != cudaSuccess) return e;
+      attr_one = true;
+    }
+    row_pass_one<LX><<<grid, block, smem, st>>>(p);
+    return cudaGetLastError();
+  }
   const size_t smem = (size_t)(1 + p.n_in) * C::RW * C::PL * sizeof(float2);
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(row_pass<LX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -15,8 +34,6 @@ static cudaError_t launch_row_t(const XParams& p, cudaStream_t st, int nz) {
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  dim3 block(C::M, C::RW);
-  dim3 grid((p.rows + C::RW - 1) / C::RW, 1, nz);
   row_pass<LX><<<grid, block, smem, st>>>(p);
   return cudaGetLastError();
 }

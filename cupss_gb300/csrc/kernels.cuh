@@ -103,13 +103,14 @@ row_pass(const XParams p) {
       continue;
     }
     const float2* in = p.in[c] + rowoff;
+    const int xcols = p.in_xcols[c] > 0 ? p.in_xcols[c] : LX;
     // the row goes through the transpose buffer once so that the mirrored element
     // X[Lx - k] of the C2R pre-processing comes from shared memory
     if (c > 0) __syncthreads();   // CTA-uniform: the previous channel's last reads of T
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       const int k = pos_step2<LX>(m, i);
-      v[i] = live ? in[k] : make_float2(0.f, 0.f);
+      v[i] = (live && k < xcols) ? in[k] : make_float2(0.f, 0.f);
       T[pad_pos<LX>(k)] = v[i];
     }
     __syncthreads();
@@ -181,13 +182,96 @@ row_pass(const XParams p) {
   }
 }
 
+// Single spectral input, single spectral product (the Cahn-Hilliard form phi^n): the
+// inverse transform of the row stays in registers and feeds the product and the forward
+// transform directly, so shared memory holds only the transpose buffer (one slot instead
+// of two) and the input is read once instead of once per factor.  Columns at or beyond
+// in_xcols[0] are known zero (dealiased channel) and are not loaded.
+template <int LX>
+struct RowOneCfg {
+  // resident CTAs per SM the register budget is sized for (RW*M = 128 threads each)
+  static constexpr int kMinBlocks = (LX <= 256) ? 4 : 2;
+};
+
+template <int LX>
+__global__ void __launch_bounds__(RowCfg<LX>::M * RowCfg<LX>::RW, RowOneCfg<LX>::kMinBlocks)
+row_pass_one(const XParams p) {
+  using C = RowCfg<LX>;
+  constexpr int M = C::M, R = C::R, PL = C::PL, RW = C::RW;
+  extern __shared__ float2 smem[];
+  if (p.members && !p.members[blockIdx.z].active) return;   // CTA-uniform
+  const int m = threadIdx.x;
+  const int rl = threadIdx.y;
+  const int row = blockIdx.x * RW + rl;
+  const bool live = row < p.rows;
+  const int sx = 2 * LX;
+  float2* T = smem + rl * PL;
+  const size_t rowoff = (size_t)blockIdx.z * p.mstride + (size_t)(live ? row : 0) * LX;
+  const int xcols = p.in_xcols[0] > 0 ? p.in_xcols[0] : LX;
+  float2 v[R];
+  const float2* in = p.in[0] + rowoff;
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int k = pos_step2<LX>(m, i);
+    v[i] = (live && k < xcols) ? in[k] : make_float2(0.f, 0.f);
+    T[pad_pos<LX>(k)] = v[i];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int k = pos_step2<LX>(m, i);
+    v[i] = c2r_pre(v[i], T[pad_pos<LX>((LX - k) & (LX - 1))], k, sx, p.tw);
+  }
+  inv_step2<LX>(v);
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < R; ++i) T[pad_pos<LX>(pos_t2<LX>(m, i))] = v[i];
+  __syncthreads();
+#pragma unroll
+  for (int s = 0; s < R; ++s) v[s] = T[pad_pos<LX>(pos_t1<LX>(m, s))];
+  inv_step1<LX>(v, m, p.tw);
+  // v[r] = real pair (r[2n], r[2n+1]) at n = m + M r: raise to the product's order
+  const int order = p.prod_n[0];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const float2 x = v[r];
+    float2 acc = make_float2(p.out_scale, p.out_scale);
+    for (int t = 0; t < order; ++t) {
+      acc.x *= x.x;
+      acc.y *= x.y;
+    }
+    v[r] = acc;
+  }
+  fwd_step1<LX>(v, m, p.tw);
+  __syncthreads();
+#pragma unroll
+  for (int s = 0; s < R; ++s) T[pad_pos<LX>(pos_t1<LX>(m, s))] = v[s];
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < R; ++i) v[i] = T[pad_pos<LX>(pos_t2<LX>(m, i))];
+  fwd_step2<LX>(v);
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < R; ++i) T[pad_pos<LX>(pos_step2<LX>(m, i))] = v[i];
+  __syncthreads();
+  float2* out = reinterpret_cast<float2*>(p.out[0]) + rowoff;
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int k = pos_step2<LX>(m, i);
+    const float2 zm = T[pad_pos<LX>((LX - k) & (LX - 1))];
+    const float2 x = r2c_post(v[i], zm, k, sx, p.tw);
+    if (live) out[k] = x;
+  }
+}
+
 // ------------------------------------------------------------------------------------
 // line pass (strided axis): forward or inverse FFT of whole lines, in place or not
 // ------------------------------------------------------------------------------------
 // Grid: x = kx' tile (W columns), y = z (kGeoY3) / ky (kGeoZ3).  Block: (W, M, 1).
-// smem: PL * W float2 (one transpose slot).
+// smem: PL * W float2 (one transpose slot).  Lines up to 256 fit the register budget of
+// four resident CTAs per SM (64 registers, no spills), longer ones that of two.
 template <int L>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, (L <= 256) ? 4 : 2)
 line_pass(const LineParams P) {
   constexpr int M = LineCfg<L>::M, R = LineCfg<L>::R;
   extern __shared__ float2 smem[];

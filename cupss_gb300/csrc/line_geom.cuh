@@ -25,11 +25,12 @@ struct LineGeom {
   int W, w, m, l, kx0, kxp, lineky;
   bool ok;
   int lofs, pstride;     // element offset of this thread's line (position 0) and stride, within a member
-  size_t mbase, slot_sz;
-  __device__ __forceinline__ explicit LineGeom(const LineParams& P) { init(P, blockIdx.x, blockIdx.y); }
-  // Explicit tile coordinates (persistent kernels): tx = kx' tile, ty = line index.
-  __device__ __forceinline__ LineGeom(const LineParams& P, int tx, int ty) { init(P, tx, ty); }
-  __device__ __forceinline__ void init(const LineParams& P, int tx, int ty) {
+  size_t mbase;
+  int slot_sz;
+  __device__ __forceinline__ explicit LineGeom(const LineParams& P) { init(P, P.sy, P.sx / 2, blockIdx.x, blockIdx.y); }
+  // Grid sizes from the caller (compile-time constants in generated kernels).
+  __device__ __forceinline__ LineGeom(const LineParams& P, int sy, int Lx) { init(P, sy, Lx, blockIdx.x, blockIdx.y); }
+  __device__ __forceinline__ void init(const LineParams& P, int sy, int Lx, int tx, int ty) {
     W = P.W;
     w = threadIdx.x;
     m = threadIdx.y;
@@ -38,27 +39,28 @@ struct LineGeom {
     kxp = kx0 + w;
     lineky = 0;
     bool lineok = true;
-    const int Lx = P.Lx;
-    if (P.geo == kGeoCol) {
+    // the paired form (NL = 2) is only used along z
+    const int geo = (NL == 2) ? (int)kGeoZ3 : P.geo;
+    if (geo == kGeoCol) {
       lofs = kxp;
       pstride = Lx;
-    } else if (P.geo == kGeoY3) {
-      lofs = ty * P.sy * Lx + kxp;
+    } else if (geo == kGeoY3) {
+      lofs = ty * sy * Lx + kxp;
       pstride = Lx;
     } else {
       if (NL == 2) {
         const int pr = ty;
-        lineky = (l == 0) ? pr : ((pr == 0) ? P.sy / 2 : P.sy - pr);
-        lineok = !(l == 1 && P.sy == 1);
+        lineky = (l == 0) ? pr : ((pr == 0) ? sy / 2 : sy - pr);
+        lineok = !(l == 1 && sy == 1);
       } else {
         lineky = ty;
       }
       lofs = lineky * Lx + kxp;
-      pstride = P.sy * Lx;
+      pstride = sy * Lx;
     }
     ok = (kxp < Lx) && lineok;
     mbase = (size_t)blockIdx.z * P.mstride;
-    slot_sz = (size_t)NL * PL * W;
+    slot_sz = NL * PL * W;
   }
   // 32-bit element index within the member; at(p) is p moved to this CTA's member.
   __device__ __forceinline__ int elem(int pos) const { return lofs + pos * pstride; }
@@ -66,9 +68,7 @@ struct LineGeom {
   __device__ __forceinline__ T* at(T* p) const {
     return p + mbase;
   }
-  __device__ __forceinline__ size_t sidx(int line, int pos) const {
-    return (size_t)(line * PL + pad_pos<L>(pos)) * W + w;
-  }
+  __device__ __forceinline__ int sidx(int line, int pos) const { return (line * PL + pad_pos<L>(pos)) * W + w; }
 };
 
 }  // namespace cupssgb

@@ -14,22 +14,29 @@ struct VPoint {
   float qx, qy, qz, q2;
 };
 
+// Grid sizes as the per-mode math sees them.  Kernels generated for one system fill
+// them with compile-time constants, so that every index expression below folds.
+struct Dims {
+  int sx, sy, sz;
+};
+__device__ __forceinline__ Dims dims_of(const LineParams& P) { return Dims{P.sx, P.sy, P.sz}; }
+
 __device__ __forceinline__ float q_of(int k, int n, float step) {
   return (float)(k < (n + 1) / 2 ? k : k - n) * step;   // src/field_init.cpp:248-250
 }
 
-__device__ __forceinline__ VPoint make_vpoint(const LineParams& P, int kx, int ky, int kz) {
+__device__ __forceinline__ VPoint make_vpoint(const LineParams& P, const Dims& d, int kx, int ky, int kz) {
   VPoint vp;
   vp.kx = kx;
   vp.ky = ky;
   vp.kz = kz;
   vp.origin = (kx == 0 && ky == 0 && kz == 0);
-  vp.nyx = (P.sx > 1) && (2 * kx == P.sx);
-  vp.nyy = (P.sy > 1) && (2 * ky == P.sy);
-  vp.nyz = (P.sz > 1) && (2 * kz == P.sz);
-  vp.qx = q_of(kx, P.sx, P.stepqx);
-  vp.qy = q_of(ky, P.sy, P.stepqy);
-  vp.qz = q_of(kz, P.sz, P.stepqz);
+  vp.nyx = (d.sx > 1) && (2 * kx == d.sx);
+  vp.nyy = (d.sy > 1) && (2 * ky == d.sy);
+  vp.nyz = (d.sz > 1) && (2 * kz == d.sz);
+  vp.qx = q_of(kx, d.sx, P.stepqx);
+  vp.qy = q_of(ky, d.sy, P.stepqy);
+  vp.qz = q_of(kz, d.sz, P.stepqz);
   vp.q2 = vp.qx * vp.qx + vp.qy * vp.qy + vp.qz * vp.qz;
   return vp;
 }
@@ -119,14 +126,14 @@ __device__ __forceinline__ float noise_amp(const LineParams& P, int fi, const VP
 //    mode at t + Lt/2 -- one generator call for two modes of the same thread;
 //  * modes on the kx = 0 and kx = sx/2 planes: c = the smaller linear index of the
 //    Hermitian pair (k, -k), words 0,1; the other member takes the conjugate.
-__device__ __forceinline__ int line_axis_len(const LineParams& P) {
-  return P.sz > 1 ? P.sz : (P.sy > 1 ? P.sy : 1);
+__device__ __forceinline__ int line_axis_len(const Dims& d) {
+  return d.sz > 1 ? d.sz : (d.sy > 1 ? d.sy : 1);
 }
 
 // Both modes (t, t + Lt/2) of a folded pair, t < Lt/2, 0 < kx < sx/2.
-__device__ __forceinline__ void noise_pair(const LineParams& P, const NoiseKey& nk, int fid, int kx, int ky,
-                                           int kz, float2& lo, float2& hi) {
-  const uint32_t lin = ((uint32_t)kz * P.sy + ky) * P.sx + kx;
+__device__ __forceinline__ void noise_pair(const LineParams& P, const Dims& d, const NoiseKey& nk, int fid, int kx,
+                                           int ky, int kz, float2& lo, float2& hi) {
+  const uint32_t lin = ((uint32_t)kz * d.sy + ky) * d.sx + kx;
   float g1, g2, g3, g4;
   philox_normal4(lin, nk.step, (uint32_t)fid, nk.key0, nk.key1, g1, g2, g3, g4);
   lo = make_float2(P.sqrtHalfN * g1, P.sqrtHalfN * g2);
@@ -134,27 +141,27 @@ __device__ __forceinline__ void noise_pair(const LineParams& P, const NoiseKey& 
 }
 
 // Any mode with kx <= sx/2.
-__device__ __forceinline__ float2 noise_at(const LineParams& P, const NoiseKey& nk, int fid, int kx, int ky,
-                                           int kz) {
-  if (kx != 0 && 2 * kx != P.sx) {
-    const int Lt = line_axis_len(P);
+__device__ __forceinline__ float2 noise_at(const LineParams& P, const Dims& d, const NoiseKey& nk, int fid, int kx,
+                                           int ky, int kz) {
+  if (kx != 0 && 2 * kx != d.sx) {
+    const int Lt = line_axis_len(d);
     if (Lt == 1) {
       float2 lo, hi;
-      noise_pair(P, nk, fid, kx, ky, kz, lo, hi);
+      noise_pair(P, d, nk, fid, kx, ky, kz, lo, hi);
       return lo;
     }
     const int h = Lt / 2;
-    int& t = (P.sz > 1) ? kz : ky;
+    int& t = (d.sz > 1) ? kz : ky;
     const bool upper = t >= h;
     if (upper) t -= h;
     float2 lo, hi;
-    noise_pair(P, nk, fid, kx, ky, kz, lo, hi);
+    noise_pair(P, d, nk, fid, kx, ky, kz, lo, hi);
     return upper ? hi : lo;
   }
-  const uint32_t lin = ((uint32_t)kz * P.sy + ky) * P.sx + kx;
-  const int pky = (P.sy - ky) & (P.sy - 1);
-  const int pkz = (P.sz - kz) & (P.sz - 1);
-  const uint32_t plin = ((uint32_t)pkz * P.sy + pky) * P.sx + kx;
+  const uint32_t lin = ((uint32_t)kz * d.sy + ky) * d.sx + kx;
+  const int pky = (d.sy - ky) & (d.sy - 1);
+  const int pkz = (d.sz - kz) & (d.sz - 1);
+  const uint32_t plin = ((uint32_t)pkz * d.sy + pky) * d.sx + kx;
   uint32_t ctr = lin;
   bool conj = false;
   float g1, g2;
@@ -174,9 +181,9 @@ __device__ __forceinline__ bool keep_axis(int k, int n, int lim) {
   const int nk = (k > (n >> 1)) ? n - k : k;
   return nk <= lim;
 }
-__device__ __forceinline__ bool keep_point(const LineParams& P, const VPoint& vp, const FieldK& F) {
-  return keep_axis(vp.kx, P.sx, F.chan_xlimit) && keep_axis(vp.ky, P.sy, F.chan_ylimit) &&
-         keep_axis(vp.kz, P.sz, F.chan_zlimit);
+__device__ __forceinline__ bool keep_point(const Dims& d, const VPoint& vp, const FieldK& F) {
+  return keep_axis(vp.kx, d.sx, F.chan_xlimit) && keep_axis(vp.ky, d.sy, F.chan_ylimit) &&
+         keep_axis(vp.kz, d.sz, F.chan_zlimit);
 }
 
 // Unpacks component `which` (0: kx = 0 plane, 1: kx = sx/2 plane) of a packed value.

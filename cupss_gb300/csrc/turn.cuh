@@ -15,8 +15,14 @@
 //
 // Shared-memory slots (each NL * PL * W float2):
 //   [0, n_prod)                 forward-transformed products (step-2 positions)
-//   [n_prod, n_prod+src_slots)  prefetched states read by the field being updated
-//   [n_prod+src_slots]          dealiased copy being inverse-transformed
+//   [n_prod, n_prod+src_slots)  states read by the field being updated, copied in
+//                               asynchronously (cp.async) while earlier work runs
+//   tslot                       transpose buffer of the inverse transform of the dealiased
+//                               copy: slot 0 when the phase has one field (every read of
+//                               the other slots is done by then), else a slot of its own
+//                               so that the next field's states can be copied in meanwhile.
+// The dealiased copy itself stays in registers between the update and its inverse
+// transform.
 #pragma once
 #include "engine_types.h"
 #include "fft.cuh"
@@ -25,32 +31,49 @@
 
 namespace cupssgb {
 
-// Source access at one mode: self and Hermitian-partner shared-memory addresses;
-// wsel >= 0 selects the unpacked component on the packed column.
-// States come either from prefetch slots (src_direct == false) or straight from the
-// phase-start state arrays at global elements es / ep.  xi is the Fourier-space noise
+// 8-byte asynchronous global -> shared copy (zero-filled when src_bytes is 0, in which
+// case nothing is read).
+__device__ __forceinline__ void cp_async8(float2* sdst, const float2* gsrc, int src_bytes) {
+  unsigned sa;
+  asm volatile("{ .reg .u64 t; cvta.to.shared.u64 t, %1; cvt.u32.u64 %0, t; }" : "=r"(sa) : "l"(sdst));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(sa), "l"(gsrc), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Issues the copies of every state field F reads into its prefetch slots, at the
+// thread's step-2 positions (zeros outside the grid).
+template <int L, class G>
+__device__ __forceinline__ void prefetch_states(const LineParams& P, const FieldK& F, const G& g, float2* smem,
+                                                int slot_sz) {
+  constexpr int R = LineCfg<L>::R;
+  for (int j = 0; j < F.nsrc; ++j) {
+    float2* Sj = smem + (P.n_prod + j) * slot_sz;
+    const float2* st = g.at(P.state[F.src[j]]);
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int pos = pos_step2<L>(g.m, i);
+      cp_async8(Sj + g.sidx(g.l, pos), g.ok ? st + g.elem(pos) : st, g.ok ? 8 : 0);
+    }
+  }
+  cp_async_commit();
+}
+
+// Source access at one mode: self and Hermitian-partner shared-memory indices; wsel >= 0
+// selects the unpacked component on the packed column.  xi is the Fourier-space noise
 // sample of the mode (used by noisy fields).
 struct Fetch {
   const float2* smem;
-  size_t slot_sz, as, ap;
+  int slot_sz, as, ap;
   int n_prod, wsel;
-  bool src_direct;
-  const float2* const* states;   // P.state
-  const int* srcs;               // F.src
-  size_t es, ep;
   float2 xi;
   __device__ __forceinline__ float2 get(int slot) const {
-    const float2* S = smem + (size_t)slot * slot_sz;
+    const float2* S = smem + slot * slot_sz;
     if (wsel < 0) return S[as];
     return unpack(S[as], S[ap], wsel);
   }
   __device__ __forceinline__ float2 prod(int c) const { return get(c); }
-  __device__ __forceinline__ float2 src(int j) const {
-    if (!src_direct) return get(n_prod + j);
-    const float2* st = states[srcs[j]];
-    if (wsel < 0) return st[es];
-    return unpack(st[es], st[ep], wsel);
-  }
+  __device__ __forceinline__ float2 src(int j) const { return get(n_prod + j); }
 };
 
 struct InterpProg {
@@ -97,34 +120,40 @@ struct InterpProg {
   }
 };
 
-// One plain (kx' > 0) mode: register index i of the thread's step-2 positions.
-template <int L, class Prog, class G>
-__device__ __forceinline__ void update_mode(const LineParams& P, const FieldK& F, int fi, const G& g, int i,
-                                            bool z3, const float2* smem, size_t slot_sz, float2* Cs,
-                                            bool has_chan, float2 xi) {
+// Structure of the phase a kernel is compiled for.  The table-driven kernel reads it
+// from the parameter block (zeros here); a generated program fixes the number of fields
+// of the phase and the grid sizes at compile time, so the field loop unrolls (static
+// parameter offsets) and every index expression of the per-mode math folds.
+struct RtSpec {
+  static constexpr int kNF = 0;
+  static constexpr int kSX = 0, kSY = 0, kSZ = 0;
+};
+
+// One plain (kx' > 0) mode: register index i of the thread's step-2 positions.  Writes
+// the new state and returns the dealiased, 1/N-scaled copy of the mode (zero when masked
+// or when the field has no dealiased copy).
+template <int L, bool Z3, class Prog, class G>
+__device__ __forceinline__ float2 update_mode(const LineParams& P, const Dims& d, const FieldK& F, int fi,
+                                              const G& g, int i, const float2* smem, bool has_chan, float2 xi) {
   const int pos = pos_step2<L>(g.m, i);
   Fetch fx;
   fx.smem = smem;
-  fx.slot_sz = slot_sz;
+  fx.slot_sz = g.slot_sz;
   fx.as = g.sidx(g.l, pos);
   fx.ap = fx.as;
   fx.n_prod = P.n_prod;
   fx.wsel = -1;
-  fx.src_direct = false;
-  fx.states = P.state;
-  fx.srcs = F.src;
-  fx.es = g.mbase + g.elem(pos);
-  fx.ep = fx.es;
   fx.xi = xi;
-  const VPoint vp = make_vpoint(P, g.kxp, z3 ? g.lineky : pos, z3 ? pos : 0);
+  const VPoint vp = make_vpoint(P, d, g.kxp, Z3 ? g.lineky : pos, Z3 ? pos : 0);
   const float2 z = Prog::eval(P, fi, vp, fx);
   g.at(F.next)[g.elem(pos)] = z;
-  if (has_chan) Cs[fx.as] = keep_point(P, vp, F) ? c_scale(z, P.invN) : make_float2(0.f, 0.f);
+  return (has_chan && keep_point(d, vp, F)) ? c_scale(z, P.invN) : make_float2(0.f, 0.f);
 }
 
-template <int L, int NL, class Prog>
+template <int L, int NL, class Prog, class Spec = RtSpec>
 __device__ __forceinline__ void turn_body(const LineParams& P) {
   constexpr int R = LineCfg<L>::R;
+  constexpr bool Z3 = (NL == 2);   // the paired z-line form is the 3D turnaround
   extern __shared__ float2 smem[];
   NoiseKey nk{P.key0, P.key1, P.step};
   if (P.members) {
@@ -132,16 +161,21 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
     if (!mk.active) return;   // CTA-uniform, before any barrier
     nk = NoiseKey{mk.key0, mk.key1, mk.step + P.step_off};
   }
-  const LineGeom<L, NL> g(P);
+  const Dims d = Spec::kSX ? Dims{Spec::kSX, Spec::kSY, Spec::kSZ} : dims_of(P);
+  const LineGeom<L, NL> g(P, d.sy, d.sx / 2);
   const int m = g.m, l = g.l;
-  const size_t slot_sz = g.slot_sz;
-  const int sy = P.sy;
-  const bool z3 = (P.geo == kGeoZ3);
+  const int slot_sz = g.slot_sz;
+  const int sy = d.sy;
+  const int nf = Spec::kNF ? Spec::kNF : P.nf;
   float2 v[R];
+
+  // 0) the states the first field reads start on their way to shared memory now, and
+  //    arrive while the products are transformed
+  if (nf > 0) prefetch_states<L>(P, P.f[0], g, smem, slot_sz);
 
   // 1) forward transform of every product channel into its slot (step-2 positions)
   for (int c = 0; c < P.n_prod; ++c) {
-    float2* Sl = smem + (size_t)c * slot_sz;
+    float2* Sl = smem + c * slot_sz;
     const float2* in = g.at(P.prod_in[c]);
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = g.ok ? in[g.elem(pos_step1<L>(m, r))] : make_float2(0.f, 0.f);
@@ -157,32 +191,23 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
     for (int i = 0; i < R; ++i) Sl[g.sidx(l, pos_step2<L>(m, i))] = v[i];
   }
 
-  float2* Cs = smem + (size_t)(P.n_prod + P.src_slots) * slot_sz;
-  for (int fi = 0; fi < P.nf; ++fi) {
+  auto field_step = [&](const int fi) {
     const FieldK& F = P.f[fi];
     const bool has_chan = (F.chan != nullptr);
-    // 2a) table-driven program: prefetch every state the update reads, all R points of
-    //     the thread at once (generated programs load them directly, unrolled)
-    for (int j = 0; j < F.nsrc; ++j) {
-      float2* Sj = smem + (size_t)(P.n_prod + j) * slot_sz;
-      const float2* st = g.at(P.state[F.src[j]]);
-#pragma unroll
-      for (int i = 0; i < R; ++i) {
-        const int pos = pos_step2<L>(m, i);
-        Sj[g.sidx(l, pos)] = g.ok ? st[g.elem(pos)] : make_float2(0.f, 0.f);
-      }
-    }
-    __syncthreads();
-    // 2b) pointwise update.  Columns kx' > 0: plain half-spectrum modes; with a
+    cp_async_wait_all();
+    __syncthreads();   // this field's states and every product slot are in place
+    // 2) pointwise update.  Columns kx' > 0: plain half-spectrum modes; with a
     // generated program (Prog::kUnroll) the R points are unrolled so that their
-    // independent arithmetic (noise draws included) overlaps.
+    // independent arithmetic overlaps, the noise draws first (independent generator
+    // calls side by side).
+    float2 ch[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) ch[i] = make_float2(0.f, 0.f);
     const int pl = (NL == 2 && sy > 1 && blockIdx.y != 0) ? (l ^ 1) : l;
     if (g.ok && g.kxp != 0) {
       if constexpr (Prog::kUnroll) {
-        // Fourier noise of the thread's R modes, drawn in (t, t + Lt/2) pairs
-        float2 xi[R];
-#pragma unroll
-        for (int i = 0; i < R; ++i) xi[i] = make_float2(0.f, 0.f);
+        // Fourier noise of the thread's R modes, drawn in (t, t + Lt/2) pairs; ch holds
+        // the noise until the update of its mode replaces it
         if (F.noisy) {
           constexpr int Mx = LineCfg<L>::M;
           constexpr int HALF = (Mx >= 2) ? Mx / 2 : R / 2;   // register offset of t + L/2
@@ -193,35 +218,41 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
             if (lower) {
               const int pos = pos_step2<L>(m, i);
               float2 lo, hi;
-              if (z3) noise_pair(P, nk, F.fid, g.kxp, g.lineky, pos, lo, hi);
-              else noise_pair(P, nk, F.fid, g.kxp, pos, 0, lo, hi);
-              xi[i] = lo;
-              if (L > 1) xi[i + HALF] = hi;
+              if (Z3) noise_pair(P, d, nk, F.fid, g.kxp, g.lineky, pos, lo, hi);
+              else noise_pair(P, d, nk, F.fid, g.kxp, pos, 0, lo, hi);
+              ch[i] = lo;
+              if (L > 1) ch[i + HALF] = hi;
             }
           }
         }
 #pragma unroll
-        for (int i = 0; i < R; ++i)
-          update_mode<L, Prog>(P, F, fi, g, i, z3, smem, slot_sz, Cs, has_chan, xi[i]);
+        for (int i = 0; i < R; ++i) ch[i] = update_mode<L, Z3, Prog>(P, d, F, fi, g, i, smem, has_chan, ch[i]);
       } else {
+        // table-driven program: a rolled loop (its unrolled code would be very large);
+        // the results go through a thread-local array into the registers
+        float2 chl[R];
 #pragma unroll 1
         for (int i = 0; i < R; ++i) {
           float2 xi = make_float2(0.f, 0.f);
           if (F.noisy) {
             const int pos = pos_step2<L>(m, i);
-            xi = z3 ? noise_at(P, nk, F.fid, g.kxp, g.lineky, pos) : noise_at(P, nk, F.fid, g.kxp, pos, 0);
+            xi = Z3 ? noise_at(P, d, nk, F.fid, g.kxp, g.lineky, pos) : noise_at(P, d, nk, F.fid, g.kxp, pos, 0);
           }
-          update_mode<L, Prog>(P, F, fi, g, i, z3, smem, slot_sz, Cs, has_chan, xi);
+          chl[i] = update_mode<L, Z3, Prog>(P, d, F, fi, g, i, smem, has_chan, xi);
         }
+#pragma unroll
+        for (int i = 0; i < R; ++i) ch[i] = chl[i];
       }
     } else if (g.ok) {
       // packed column kx' = 0: the kx = 0 and kx = sx/2 planes, unpacked with the
-      // Hermitian partner (-ky, -kz)
+      // Hermitian partner (-ky, -kz).  One thread in W of the first tile only: a rolled
+      // loop through a thread-local array keeps the common path's code small.
+      float2 chl[R];
 #pragma unroll 1
       for (int i = 0; i < R; ++i) {
         const int pos = pos_step2<L>(m, i);
-        const int ky = z3 ? g.lineky : pos;
-        const int kz = z3 ? pos : 0;
+        const int ky = Z3 ? g.lineky : pos;
+        const int kz = Z3 ? pos : 0;
         const int ppos = (L - pos) & (L - 1);
         Fetch fx;
         fx.smem = smem;
@@ -229,51 +260,53 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
         fx.as = g.sidx(l, pos);
         fx.ap = g.sidx(pl, ppos);
         fx.n_prod = P.n_prod;
-        fx.src_direct = false;
-        fx.states = P.state;
-        fx.srcs = F.src;
-        fx.es = g.mbase + g.elem(pos);
-        if (z3) fx.ep = g.mbase + (size_t)((sy - ky) & (sy - 1)) * P.Lx + (size_t)ppos * g.pstride;
-        else fx.ep = g.mbase + g.elem(ppos);
         fx.wsel = 0;
-        const VPoint v0 = make_vpoint(P, 0, ky, kz);
-        fx.xi = F.noisy ? noise_at(P, nk, F.fid, 0, ky, kz) : make_float2(0.f, 0.f);
+        const VPoint v0 = make_vpoint(P, d, 0, ky, kz);
+        fx.xi = F.noisy ? noise_at(P, d, nk, F.fid, 0, ky, kz) : make_float2(0.f, 0.f);
         const float2 o0 = Prog::eval(P, fi, v0, fx);
         fx.wsel = 1;
-        const VPoint v1 = make_vpoint(P, P.sx / 2, ky, kz);
-        fx.xi = F.noisy ? noise_at(P, nk, F.fid, P.sx / 2, ky, kz) : make_float2(0.f, 0.f);
+        const VPoint v1 = make_vpoint(P, d, d.sx / 2, ky, kz);
+        fx.xi = F.noisy ? noise_at(P, d, nk, F.fid, d.sx / 2, ky, kz) : make_float2(0.f, 0.f);
         const float2 o1 = Prog::eval(P, fi, v1, fx);
         const float2 z = c_add(o0, c_muli(o1));
-        const float2 a = (has_chan && keep_point(P, v0, F)) ? c_scale(o0, P.invN) : make_float2(0.f, 0.f);
-        const float2 b = (has_chan && keep_point(P, v1, F)) ? c_scale(o1, P.invN) : make_float2(0.f, 0.f);
+        const float2 a = (has_chan && keep_point(d, v0, F)) ? c_scale(o0, P.invN) : make_float2(0.f, 0.f);
+        const float2 b = (has_chan && keep_point(d, v1, F)) ? c_scale(o1, P.invN) : make_float2(0.f, 0.f);
         g.at(F.next)[g.elem(pos)] = z;
-        if (has_chan) Cs[g.sidx(l, pos)] = c_add(a, c_muli(b));
+        chl[i] = c_add(a, c_muli(b));
       }
+#pragma unroll
+      for (int i = 0; i < R; ++i) ch[i] = chl[i];
     }
-    // 2c) inverse transform of the dealiased copy
+    // 3) inverse transform of the dealiased copy
     bool skip = !has_chan || g.kx0 > F.chan_xlimit;
-    if (z3 && NL == 2) {
+    if (Z3) {
       // both lines of pair p >= 1 have |n_y| = p; pair 0 holds n_y = 0
       const int pr = (int)blockIdx.y;
       if (pr > 0 && pr > F.chan_ylimit) skip = true;
     }
-    __syncthreads();   // Cs written; prefetch slots free for the next field
-    if (skip) continue;   // CTA-uniform: masked tile, the channel stays zero
+    __syncthreads();   // every read of the slots is done
+    if (fi + 1 < nf) prefetch_states<L>(P, P.f[fi + 1], g, smem, slot_sz);
+    if (skip) return;   // CTA-uniform: masked tile, the channel stays zero
+    float2* Ts = smem + P.tslot * slot_sz;
+    inv_step2<L>(ch);
 #pragma unroll
-    for (int i = 0; i < R; ++i) v[i] = Cs[g.sidx(l, pos_step2<L>(m, i))];
-    inv_step2<L>(v);
+    for (int i = 0; i < R; ++i) Ts[g.sidx(l, pos_t2<L>(m, i))] = ch[i];
     __syncthreads();
 #pragma unroll
-    for (int i = 0; i < R; ++i) Cs[g.sidx(l, pos_t2<L>(m, i))] = v[i];
-    __syncthreads();
-#pragma unroll
-    for (int s = 0; s < R; ++s) v[s] = Cs[g.sidx(l, pos_t1<L>(m, s))];
-    inv_step1<L>(v, m, P.tw);
+    for (int s = 0; s < R; ++s) ch[s] = Ts[g.sidx(l, pos_t1<L>(m, s))];
+    inv_step1<L>(ch, m, P.tw);
     if (g.ok) {
 #pragma unroll
-      for (int r = 0; r < R; ++r) g.at(F.chan)[g.elem(pos_step1<L>(m, r))] = v[r];
+      for (int r = 0; r < R; ++r) g.at(F.chan)[g.elem(pos_step1<L>(m, r))] = ch[r];
     }
-    __syncthreads();   // Cs free for the next field
+    // the next field writes Ts only after its update and the barrier that follows it,
+    // which every thread reaches after its reads of Ts above
+  };
+  if constexpr (Spec::kNF > 0) {
+#pragma unroll
+    for (int fi = 0; fi < Spec::kNF; ++fi) field_step(fi);
+  } else {
+    for (int fi = 0; fi < nf; ++fi) field_step(fi);
   }
 }
 

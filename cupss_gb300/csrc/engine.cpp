@@ -253,6 +253,20 @@ void Solver::prepare() {
     }
   }
   autotune();
+  if (use_jit_) {
+    // the kernels of the tuned tile widths, compiled now rather than inside the first step
+    const int L = (dim_ == 3) ? sz_ : sy_;
+    const int nl = (dim_ == 3) ? 2 : 1;
+    for (Phase& P : phases_) {
+      if (P.fields.empty()) continue;
+      LineParams p;
+      int nslots = 0;
+      bool any_chan = false;
+      fill_turn(P, p, nslots, any_chan);
+      p.W = P.tuned_w > 0 ? P.tuned_w : pick_w(L, nl, nslots);
+      jit_kernel(turn_source(P, p, L, nl), "cupssgb_turn");
+    }
+  }
 }
 
 int Solver::pick_w(int L, int nl, int nslots) const {
@@ -287,7 +301,7 @@ void Solver::fill_line_common(LineParams& p, int L, int geo, int mode) const {
   p.tw = tw_;
 }
 
-void Solver::line_fwd_inv(int geo, int mode, const float2* in, float2* out, int xlimit, bool batch) {
+void Solver::line_fwd_inv(int geo, int mode, const float2* in, float2* out, int xlimit, bool batch, int lkeep) {
   LineParams p;
   const int L = (geo == kGeoY3 || geo == kGeoCol) ? sy_ : sz_;
   fill_line_common(p, L, geo, mode);
@@ -296,6 +310,7 @@ void Solver::line_fwd_inv(int geo, int mode, const float2* in, float2* out, int 
   p.prod_in[0] = in;
   p.prod_out[0] = out;
   p.inv_xlimit[0] = xlimit;
+  p.inv_lkeep[0] = lkeep;
   if (batch) {
     p.mstride = half_;
     p.members = members_d_;
@@ -642,7 +657,7 @@ void Solver::fill_turn(const Phase& P, LineParams& p, int& nslots, bool& any_cha
 }
 
 const std::string& Solver::turn_source(Phase& P, const LineParams& p, int L, int nl) {
-  std::vector<int> sig = {L, nl, p.nf, p.n_prod, p.sx, p.sy, p.sz};
+  std::vector<int> sig = {L, nl, p.nf, p.n_prod, p.sx, p.sy, p.sz, p.W};
   for (int fi = 0; fi < p.nf; ++fi) {
     const FieldK& K = p.f[fi];
     sig.insert(sig.end(), {K.dynamic, K.noisy, K.nterms, K.term0, K.nimp, K.imp0, K.noise_q2n, K.noise_invq,
@@ -746,7 +761,11 @@ void Solver::run_phase(Phase& P) {
   dim3 grid((Lx_ + p.W - 1) / p.W, dim_ == 3 ? std::max(sy_ / 2, 1) : 1, batch_ ? nmem_ : 1);
   mark_begin();
   if (use_jit_) {
-    const std::string& src = turn_source(P, p, L, nl);
+    // the kernel is compiled for the tuned tile width; while tuning, one width-generic
+    // kernel serves every candidate
+    LineParams ps = p;
+    if (tuning_) ps.W = 0;
+    const std::string& src = turn_source(P, ps, L, nl);
     cudaKernel_t k = jit_kernel(src, "cupssgb_turn");
     dim3 block(p.W, line_threads(L, 1, 1), nl);
     void* args[] = {(void*)&p};
@@ -762,7 +781,9 @@ void Solver::run_phase(Phase& P) {
     for (int f : P.fields)
       if (alias_order_[f] > 1) {
         mark_begin();
-        line_fwd_inv(kGeoY3, kModeInv, chanz_[f], chan_[f], sx_ / (alias_order_[f] + 1), batch_);
+        // rows |n_y| > sy/(order+1) of the z-inverted channel are masked (zero)
+        line_fwd_inv(kGeoY3, kModeInv, chanz_[f], chan_[f], sx_ / (alias_order_[f] + 1), batch_,
+                     sy_ / (alias_order_[f] + 1) + 1);
         mark_end("line_inv_y");
       }
   }

@@ -181,6 +181,7 @@ void Solver::autotune() {
   check(cudaEventCreate(&a), "cudaEventCreate");
   check(cudaEventCreate(&b), "cudaEventCreate");
   const long long l0 = launches_;
+  tuning_ = true;
   // time with every slot active (a pool may be prepared with all slots free)
   std::vector<MemberK> all = members_h_;
   for (MemberK& k : all) k.active = 1u;
@@ -222,6 +223,7 @@ void Solver::autotune() {
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
+  tuning_ = false;
   launches_ = l0;
   check(cudaMemcpyAsync(members_d_, members_h_.data(), members_h_.size() * sizeof(MemberK), cudaMemcpyHostToDevice,
                         stream_),

@@ -93,6 +93,8 @@ struct LineParams {
   const float2* prod_in[kMaxProd];
   float2* prod_out[kMaxProd];       // fwd/inv passes only (may equal prod_in)
   int inv_xlimit[kMaxProd];         // inv pass: skip tiles with kx0 > limit
+  int inv_lkeep[kMaxProd];          // inv pass: > 0 -> input positions n with |n| >= inv_lkeep
+                                    // (n = k or k - L) are known zero and not read
   int nf;
   FieldK f[kMaxPhaseFields];
   TermK term[kMaxTerms];

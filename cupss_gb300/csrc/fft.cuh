@@ -53,6 +53,16 @@ CG_HD float2 c_mulc(float2 a, float2 b) {
   return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
 }
 CG_HD float2 c_conj(float2 a) { return make_float2(a.x, -a.y); }
+
+// Butterfly sums on the paired FP32 pipe of sm_100+ (one f32x2 instruction per complex
+// add or subtract; a - b is fma(b, -1, a), exact like the scalar subtraction).
+#if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 1000)
+__device__ __forceinline__ float2 p_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 p_sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+#else
+CG_HD float2 p_add(float2 a, float2 b) { return c_add(a, b); }
+CG_HD float2 p_sub(float2 a, float2 b) { return c_sub(a, b); }
+#endif
 CG_HD float2 c_scale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 CG_HD float2 c_muli(float2 a) { return make_float2(-a.y, a.x); }    // i * a
 CG_HD float2 c_mulmi(float2 a) { return make_float2(a.y, -a.x); }   // -i * a
@@ -80,19 +90,37 @@ CG_HD float2 tw_const(float2 a) {
 // In-place DFT of the N values v[O + S*i], i in [0,N), natural-order output.
 template <int N, bool INV, int S>
 struct Dft {
-  template <int O, int K0, int... K>
-  CG_HD static void combine(float2* v, iseq<K0, K...>) {
+  // lo = e + W_N^K o, hi = e - W_N^K o.  Twiddles +-i stay on the scalar pipe, where the
+  // swap and sign fold into the additions; every other sum uses the paired pipe.
+  template <int K>
+  CG_HD static void bfly(float2& lo, float2& hi, float2 e, float2 o) {
+    constexpr int k = K % N;
+    if constexpr (k == 0) {
+      lo = p_add(e, o);
+      hi = p_sub(e, o);
+    } else if constexpr (2 * k == N) {
+      lo = p_sub(e, o);
+      hi = p_add(e, o);
+    } else if constexpr (4 * k == N || 4 * k == 3 * N) {
+      const float2 t = tw_const<N, K, INV>(o);
+      lo = c_add(e, t);
+      hi = c_sub(e, t);
+    } else {
+      const float2 t = tw_const<N, K, INV>(o);
+      lo = p_add(e, t);
+      hi = p_sub(e, t);
+    }
+  }
+  template <int O, int... K>
+  CG_HD static void combine(float2* v, iseq<K...>) {
     constexpr int H = N / 2;
-    float2 ev[H];
-#pragma unroll
-    for (int q = 0; q < H; ++q) ev[q] = v[O + 2 * S * q];
-    float2 od[H] = {tw_const<N, K0, INV>(v[O + S + 2 * S * K0]),
-                    tw_const<N, K, INV>(v[O + S + 2 * S * K])...};
+    float2 ev[H], od[H];
 #pragma unroll
     for (int q = 0; q < H; ++q) {
-      v[O + S * q] = c_add(ev[q], od[q]);
-      v[O + S * (q + H)] = c_sub(ev[q], od[q]);
+      ev[q] = v[O + 2 * S * q];
+      od[q] = v[O + S + 2 * S * q];
     }
+    (bfly<K>(v[O + S * K], v[O + S * (K + H)], ev[K], od[K]), ...);
   }
   template <int O>
   CG_HD static void run(float2* v) {
@@ -100,8 +128,8 @@ struct Dft {
       return;
     } else if constexpr (N == 2) {
       float2 a = v[O], b = v[O + S];
-      v[O] = c_add(a, b);
-      v[O + S] = c_sub(a, b);
+      v[O] = p_add(a, b);
+      v[O + S] = p_sub(a, b);
     } else {
       Dft<N / 2, INV, 2 * S>::template run<O>(v);
       Dft<N / 2, INV, 2 * S>::template run<O + S>(v);

@@ -23,6 +23,12 @@ namespace cupssgb {
 
 namespace {
 
+// Division and square root of the update programs (the implicit denominator, |q|,
+// noise amplitudes, the Box-Muller radius) use the hardware approximations (about one
+// ulp) instead of the IEEE-rounded sequences, whose range checks cost a branch and a
+// dozen instructions per mode.
+const char* const kJitFastOpts[] = {"--prec-div=false", "--prec-sqrt=false"};
+
 std::mutex g_mu;
 std::map<std::string, cudaKernel_t> g_cache;
 
@@ -146,6 +152,7 @@ std::string jit_generate_turn(const LineParams& p, int L, int NL, int min_blocks
     << "struct GenSpec {\n"
     << "  static constexpr int kNF = " << p.nf << ";\n"
     << "  static constexpr int kSX = " << p.sx << ", kSY = " << p.sy << ", kSZ = " << p.sz << ";\n"
+    << "  static constexpr int kW = " << p.W << ";\n"
     << "};\n}  // namespace cupssgb\n"
     << "extern \"C\" __global__ void __launch_bounds__(256, " << min_blocks
     << ") cupssgb_turn(const cupssgb::LineParams P) {\n"
@@ -167,8 +174,8 @@ cudaKernel_t jit_kernel(const std::string& source, const char* entry) {
   if (nvrtcCreateProgram(&prog, source.c_str(), "cupssgb_turn.cu", kJitNumHeaders, kJitHeaderSources,
                          kJitHeaderNames) != NVRTC_SUCCESS)
     throw Error(kErrCuda, "nvrtcCreateProgram failed");
-  const char* opts[] = {arch.c_str(), "--std=c++17", "-lineinfo"};
-  const nvrtcResult rc = nvrtcCompileProgram(prog, 3, opts);
+  const char* opts[] = {arch.c_str(), "--std=c++17", "-lineinfo", kJitFastOpts[0], kJitFastOpts[1]};
+  const nvrtcResult rc = nvrtcCompileProgram(prog, 5, opts);
   if (rc != NVRTC_SUCCESS) {
     size_t n = 0;
     nvrtcGetProgramLogSize(prog, &n);
@@ -199,8 +206,8 @@ std::string jit_compile_only(const std::string& source, size_t* cubin_bytes) {
   if (nvrtcCreateProgram(&prog, source.c_str(), "cupssgb_turn.cu", kJitNumHeaders, kJitHeaderSources,
                          kJitHeaderNames) != NVRTC_SUCCESS)
     return "nvrtcCreateProgram failed";
-  const char* opts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "-lineinfo"};
-  const nvrtcResult rc = nvrtcCompileProgram(prog, 3, opts);
+  const char* opts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "-lineinfo", kJitFastOpts[0], kJitFastOpts[1]};
+  const nvrtcResult rc = nvrtcCompileProgram(prog, 5, opts);
   size_t n = 0;
   nvrtcGetProgramLogSize(prog, &n);
   std::string log(n, '\0');

@@ -9,7 +9,9 @@
 namespace cupssgb {
 
 // CUDA source of the turnaround kernel `cupssgb_turn` specialised to the update
-// program described by p (its fields, terms and prefactor exponents), L, NL.
+// program described by p (its fields, terms and prefactor exponents), the grid
+// (p.sx, p.sy, p.sz), L, NL, and, when p.W > 0, the tile width (p.W = 0: the width
+// is read from the parameter block at run time).
 // min_blocks: the minimum resident CTAs per SM requested from the compiler.
 // batched: numerical values come from the batch member's row of P.mvals.
 std::string jit_generate_turn(const LineParams& p, int L, int NL, int min_blocks = 2, bool batched = false);

@@ -299,8 +299,13 @@ line_pass(const LineParams P) {
         for (int i = 0; i < R; ++i) out[g.elem(pos_step2<L>(g.m, i))] = v[i];
       }
     } else {
+      const int keep = P.inv_lkeep[c];
 #pragma unroll
-      for (int i = 0; i < R; ++i) v[i] = g.ok ? in[g.elem(pos_step2<L>(g.m, i))] : make_float2(0.f, 0.f);
+      for (int i = 0; i < R; ++i) {
+        const int k = pos_step2<L>(g.m, i);
+        const int nk = (k > L / 2) ? L - k : k;
+        v[i] = (g.ok && (keep <= 0 || nk < keep)) ? in[g.elem(k)] : make_float2(0.f, 0.f);
+      }
       inv_step2<L>(v);
       __syncthreads();
 #pragma unroll

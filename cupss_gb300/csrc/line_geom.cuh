@@ -19,7 +19,9 @@
 
 namespace cupssgb {
 
-template <int L, int NL>
+// WT > 0: the tile width is a compile-time constant (generated kernels), so every
+// shared-memory index below is a per-thread base plus an immediate offset.
+template <int L, int NL, int WT = 0>
 struct LineGeom {
   static constexpr int PL = padded_len<L>();
   int W, w, m, l, kx0, kxp, lineky;
@@ -31,7 +33,7 @@ struct LineGeom {
   // Grid sizes from the caller (compile-time constants in generated kernels).
   __device__ __forceinline__ LineGeom(const LineParams& P, int sy, int Lx) { init(P, sy, Lx, blockIdx.x, blockIdx.y); }
   __device__ __forceinline__ void init(const LineParams& P, int sy, int Lx, int tx, int ty) {
-    W = P.W;
+    W = WT > 0 ? WT : P.W;
     w = threadIdx.x;
     m = threadIdx.y;
     l = threadIdx.z;

@@ -127,6 +127,7 @@ struct InterpProg {
 struct RtSpec {
   static constexpr int kNF = 0;
   static constexpr int kSX = 0, kSY = 0, kSZ = 0;
+  static constexpr int kW = 0;   // tile width (0: P.W)
 };
 
 // One plain (kx' > 0) mode: register index i of the thread's step-2 positions.  Writes
@@ -162,7 +163,7 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
     nk = NoiseKey{mk.key0, mk.key1, mk.step + P.step_off};
   }
   const Dims d = Spec::kSX ? Dims{Spec::kSX, Spec::kSY, Spec::kSZ} : dims_of(P);
-  const LineGeom<L, NL> g(P, d.sy, d.sx / 2);
+  const LineGeom<L, NL, Spec::kW> g(P, d.sy, d.sx / 2);
   const int m = g.m, l = g.l;
   const int slot_sz = g.slot_sz;
   const int sy = d.sy;

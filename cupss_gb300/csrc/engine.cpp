@@ -32,6 +32,7 @@ Solver::Solver(int sx, int sy, int sz, float dx, float dy, float dz, float dt)
   // turnaround launch shape: tile width and resident CTAs per SM (tuning knobs)
   if (const char* w = std::getenv("CUPSSGB_TURN_W")) turn_w_ = std::atoi(w);
   if (const char* b = std::getenv("CUPSSGB_TURN_MINB")) turn_min_blocks_ = std::max(1, std::atoi(b));
+  if (const char* d = std::getenv("CUPSSGB_PDL")) pdl_ = std::string(d) != "0";
   if (!pow2(sx) || sx < 2 || sx > 2048 || !pow2(sy) || sy > 1024 || !pow2(sz) || sz > 1024)
     throw Error(kErrUnsupported,
                 "grid sizes must be powers of two: 2 <= sx <= 2048, 1 <= sy, sz <= 1024");
@@ -301,7 +302,8 @@ void Solver::fill_line_common(LineParams& p, int L, int geo, int mode) const {
   p.tw = tw_;
 }
 
-void Solver::line_fwd_inv(int geo, int mode, const float2* in, float2* out, int xlimit, bool batch, int lkeep) {
+void Solver::line_fwd_inv(int geo, int mode, const float2* in, float2* out, int xlimit, bool batch, int lkeep,
+                          bool pdl) {
   LineParams p;
   const int L = (geo == kGeoY3 || geo == kGeoCol) ? sy_ : sz_;
   fill_line_common(p, L, geo, mode);
@@ -315,8 +317,10 @@ void Solver::line_fwd_inv(int geo, int mode, const float2* in, float2* out, int 
     p.mstride = half_;
     p.members = members_d_;
   }
-  dim3 grid((Lx_ + p.W - 1) / p.W, geo == kGeoY3 ? sz_ : (geo == kGeoZ3 ? sy_ : 1), batch ? nmem_ : 1);
-  check(launch_line_pass(p, 1, 1, grid, stream_), "line pass");
+  int tiles = (Lx_ + p.W - 1) / p.W;
+  if (mode == kModeInv) tiles = std::min(tiles, xlimit / p.W + 1);   // tiles past the limit stay zero
+  dim3 grid(tiles, geo == kGeoY3 ? sz_ : (geo == kGeoZ3 ? sy_ : 1), batch ? nmem_ : 1);
+  check(launch_line_pass(p, 1, 1, grid, stream_, pdl), "line pass");
   ++launches_;
 }
 
@@ -730,13 +734,13 @@ void Solver::run_phase(Phase& P) {
     x.members = members_d_;
     if (batch_) x.mstride = half_;
     mark_begin();
-    check(launch_row_pass(x, stream_, batch_ ? nmem_ : 1), "row pass");
+    check(launch_row_pass(x, stream_, batch_ ? nmem_ : 1, pdl_), "row pass");
     mark_end("row_pass");
     ++launches_;
     if (dim_ == 3) {
       for (size_t q = 0; q < P.products.size(); ++q) {
         mark_begin();
-        line_fwd_inv(kGeoY3, kModeFwd, P.prodbuf[q], P.prodbuf[q], Lx_, batch_);
+        line_fwd_inv(kGeoY3, kModeFwd, P.prodbuf[q], P.prodbuf[q], Lx_, batch_, 0, pdl_);
         mark_end("line_fwd_y");
       }
     }
@@ -769,10 +773,10 @@ void Solver::run_phase(Phase& P) {
     cudaKernel_t k = jit_kernel(src, "cupssgb_turn");
     dim3 block(p.W, line_threads(L, 1, 1), nl);
     void* args[] = {(void*)&p};
-    check(cudaLaunchKernel((const void*)k, grid, block, args, line_pass_smem(L, nl, p.W, nslots), stream_),
-          "turnaround (generated)");
+    LaunchCfg lc(grid, block, line_pass_smem(L, nl, p.W, nslots), stream_, pdl_);
+    check(cudaLaunchKernelExC(&lc.cfg, (const void*)k, args), "turnaround (generated)");
   } else {
-    check(launch_line_pass(p, nl, nslots, grid, stream_), "turnaround");
+    check(launch_line_pass(p, nl, nslots, grid, stream_, pdl_), "turnaround");
   }
   mark_end(dim_ == 3 ? "turnaround_z" : "turnaround_y");
   ++launches_;
@@ -783,7 +787,7 @@ void Solver::run_phase(Phase& P) {
         mark_begin();
         // rows |n_y| > sy/(order+1) of the z-inverted channel are masked (zero)
         line_fwd_inv(kGeoY3, kModeInv, chanz_[f], chan_[f], sx_ / (alias_order_[f] + 1), batch_,
-                     sy_ / (alias_order_[f] + 1) + 1);
+                     sy_ / (alias_order_[f] + 1) + 1, pdl_);
         mark_end("line_inv_y");
       }
   }
@@ -875,7 +879,7 @@ void Solver::step_once(uint32_t off, bool tick) {
   run_phase(phases_[1]);
   step_off_ = 0;
   if (tick) {
-    check(launch_tick(members_d_, nmem_, off + 1u, stream_), "member step count");
+    check(launch_tick(members_d_, nmem_, off + 1u, stream_, pdl_), "member step count");
     ++launches_;
   }
   ++step_;

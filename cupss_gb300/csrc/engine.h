@@ -154,7 +154,7 @@ class Solver {
   int pick_w(int L, int nl, int nslots) const;
   // lkeep > 0: inverse-pass input positions with |n| >= lkeep along the line are zero
   void line_fwd_inv(int geo, int mode, const float2* in, float2* out, int xlimit, bool batch = false,
-                    int lkeep = 0);
+                    int lkeep = 0, bool pdl = false);
   void to_real_scratch(int f, int m);
   void step_once(uint32_t off, bool tick);
   // batches
@@ -186,6 +186,7 @@ class Solver {
   int turn_w_ = 0;            // 0: automatic tile width
   int turn_min_blocks_ = 2;   // __launch_bounds__ min blocks of the generated turnaround
   bool tuning_ = false;       // autotune in progress: run the width-generic generated kernel
+  bool pdl_ = true;           // step kernels use programmatic dependent launch
   long long step_ = 0;
   long long launches_ = 0;
   size_t dev_bytes_ = 0;

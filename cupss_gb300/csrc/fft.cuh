@@ -54,6 +54,21 @@ CG_HD float2 c_mulc(float2 a, float2 b) {
 }
 CG_HD float2 c_conj(float2 a) { return make_float2(a.x, -a.y); }
 
+// Programmatic dependent launch.  A step kernel launched with programmatic stream
+// serialization may become resident while its predecessor in the stream drains.  At its
+// top it lets its own successor launch (all of its CTAs are running by the time that
+// fires) and then waits until the predecessor grid has completed and its memory is
+// visible, before touching global memory.  Both are no-ops for a kernel launched without
+// the attribute.
+#if defined(__CUDACC__)
+__device__ __forceinline__ void grid_dep_sync() {
+#if defined(__CUDA_ARCH__)
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+#endif
+}
+#endif
+
 // Butterfly sums on the paired FP32 pipe of sm_100+ (one f32x2 instruction per complex
 // add or subtract; a - b is fma(b, -1, a), exact like the scalar subtraction).
 #if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 1000)

@@ -17,20 +17,20 @@ static cudaError_t set_smem_attr(K kernel, bool& done) {
 #define CUPSSGB_LINE_INST(L)                                                                    \
   namespace cupssgb {                                                                           \
   cudaError_t launch_line_##L(const LineParams& p, int nl, size_t smem, dim3 grid,              \
-                              cudaStream_t st) {                                                \
+                              cudaStream_t st, bool pdl) {                                      \
     static bool a0 = false, a1 = false, a2 = false;                                             \
-    dim3 block(p.W, LineCfg<L>::M, nl);                                                         \
+    LaunchCfg lc(grid, dim3(p.W, LineCfg<L>::M, nl), smem, st, pdl);                            \
     cudaError_t e = cudaSuccess;                                                                \
     if (p.mode != kModeTurn) {                                                                  \
       e = set_smem_attr(line_pass<L>, a0);                                                      \
-      if (e == cudaSuccess) line_pass<L><<<grid, block, smem, st>>>(p);                         \
+      if (e == cudaSuccess) e = cudaLaunchKernelEx(&lc.cfg, line_pass<L>, p);                   \
     } else if (nl == 2) {                                                                       \
       e = set_smem_attr(turn_pass<L, 2>, a2);                                                   \
-      if (e == cudaSuccess) turn_pass<L, 2><<<grid, block, smem, st>>>(p);                      \
+      if (e == cudaSuccess) e = cudaLaunchKernelEx(&lc.cfg, turn_pass<L, 2>, p);                \
     } else {                                                                                    \
       e = set_smem_attr(turn_pass<L, 1>, a1);                                                   \
-      if (e == cudaSuccess) turn_pass<L, 1><<<grid, block, smem, st>>>(p);                      \
+      if (e == cudaSuccess) e = cudaLaunchKernelEx(&lc.cfg, turn_pass<L, 1>, p);                \
     }                                                                                           \
-    return e != cudaSuccess ? e : cudaGetLastError();                                          \
+    return e;                                                                                   \
   }                                                                                             \
   }

@@ -16,20 +16,20 @@ size_t line_pass_smem(int L, int nl, int W, int nslots) {
 }
 int line_threads(int L, int nl, int W) { return W * m_of(L) * nl; }
 
-cudaError_t launch_line_pass(const LineParams& p, int nl, int nslots, dim3 grid, cudaStream_t st) {
+cudaError_t launch_line_pass(const LineParams& p, int nl, int nslots, dim3 grid, cudaStream_t st, bool pdl) {
   const size_t smem = line_pass_smem(p.L, nl, p.W, nslots > 0 ? nslots : 1);
   switch (p.L) {
-    case 1: return launch_line_1(p, nl, smem, grid, st);
-    case 2: return launch_line_2(p, nl, smem, grid, st);
-    case 4: return launch_line_4(p, nl, smem, grid, st);
-    case 8: return launch_line_8(p, nl, smem, grid, st);
-    case 16: return launch_line_16(p, nl, smem, grid, st);
-    case 32: return launch_line_32(p, nl, smem, grid, st);
-    case 64: return launch_line_64(p, nl, smem, grid, st);
-    case 128: return launch_line_128(p, nl, smem, grid, st);
-    case 256: return launch_line_256(p, nl, smem, grid, st);
-    case 512: return launch_line_512(p, nl, smem, grid, st);
-    case 1024: return launch_line_1024(p, nl, smem, grid, st);
+    case 1: return launch_line_1(p, nl, smem, grid, st, pdl);
+    case 2: return launch_line_2(p, nl, smem, grid, st, pdl);
+    case 4: return launch_line_4(p, nl, smem, grid, st, pdl);
+    case 8: return launch_line_8(p, nl, smem, grid, st, pdl);
+    case 16: return launch_line_16(p, nl, smem, grid, st, pdl);
+    case 32: return launch_line_32(p, nl, smem, grid, st, pdl);
+    case 64: return launch_line_64(p, nl, smem, grid, st, pdl);
+    case 128: return launch_line_128(p, nl, smem, grid, st, pdl);
+    case 256: return launch_line_256(p, nl, smem, grid, st, pdl);
+    case 512: return launch_line_512(p, nl, smem, grid, st, pdl);
+    case 1024: return launch_line_1024(p, nl, smem, grid, st, pdl);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -108,13 +108,14 @@ __global__ void mask_spectrum(const MaskParams p) {
 }
 
 __global__ void tick_members(MemberK* m, int n, uint32_t inc) {
+  grid_dep_sync();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n && m[i].active) m[i].step += inc;
 }
 
-cudaError_t launch_tick(MemberK* members, int n, uint32_t inc, cudaStream_t st) {
-  tick_members<<<(n + 255) / 256, 256, 0, st>>>(members, n, inc);
-  return cudaGetLastError();
+cudaError_t launch_tick(MemberK* members, int n, uint32_t inc, cudaStream_t st, bool pdl) {
+  LaunchCfg lc(dim3((n + 255) / 256), dim3(256), 0, st, pdl);
+  return cudaLaunchKernelEx(&lc.cfg, tick_members, members, n, inc);
 }
 
 cudaError_t launch_compress(const CompressParams& p, cudaStream_t st) {

@@ -11,7 +11,7 @@ static bool row_is_one(const XParams& p) {
 }
 
 template <int LX>
-static cudaError_t launch_row_t(const XParams& p, cudaStream_t st, int nz) {
+static cudaError_t launch_row_t(const XParams& p, cudaStream_t st, int nz, bool pdl) {
   using C = RowCfg<LX>;
   static bool attr = false, attr_one = false;
   dim3 block(C::M, C::RW);
@@ -24,8 +24,8 @@ static cudaError_t launch_row_t(const XParams& p, cudaStream_t st, int nz) {
       if (e != cudaSuccess) return e;
       attr_one = true;
     }
-    row_pass_one<LX><<<grid, block, smem, st>>>(p);
-    return cudaGetLastError();
+    LaunchCfg lc(grid, block, smem, st, pdl);
+    return cudaLaunchKernelEx(&lc.cfg, row_pass_one<LX>, p);
   }
   const size_t smem = (size_t)(1 + p.n_in) * C::RW * C::PL * sizeof(float2);
   if (!attr) {
@@ -34,8 +34,8 @@ static cudaError_t launch_row_t(const XParams& p, cudaStream_t st, int nz) {
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  row_pass<LX><<<grid, block, smem, st>>>(p);
-  return cudaGetLastError();
+  LaunchCfg lc(grid, block, smem, st, pdl);
+  return cudaLaunchKernelEx(&lc.cfg, row_pass<LX>, p);
 }
 
 template <int LX>
@@ -44,19 +44,19 @@ static size_t row_smem_t(int n_in) {
   return (size_t)(1 + n_in) * C::RW * C::PL * sizeof(float2);
 }
 
-cudaError_t launch_row_pass(const XParams& p, cudaStream_t st, int nz) {
+cudaError_t launch_row_pass(const XParams& p, cudaStream_t st, int nz, bool pdl) {
   switch (p.Lx) {
-    case 1: return launch_row_t<1>(p, st, nz);
-    case 2: return launch_row_t<2>(p, st, nz);
-    case 4: return launch_row_t<4>(p, st, nz);
-    case 8: return launch_row_t<8>(p, st, nz);
-    case 16: return launch_row_t<16>(p, st, nz);
-    case 32: return launch_row_t<32>(p, st, nz);
-    case 64: return launch_row_t<64>(p, st, nz);
-    case 128: return launch_row_t<128>(p, st, nz);
-    case 256: return launch_row_t<256>(p, st, nz);
-    case 512: return launch_row_t<512>(p, st, nz);
-    case 1024: return launch_row_t<1024>(p, st, nz);
+    case 1: return launch_row_t<1>(p, st, nz, pdl);
+    case 2: return launch_row_t<2>(p, st, nz, pdl);
+    case 4: return launch_row_t<4>(p, st, nz, pdl);
+    case 8: return launch_row_t<8>(p, st, nz, pdl);
+    case 16: return launch_row_t<16>(p, st, nz, pdl);
+    case 32: return launch_row_t<32>(p, st, nz, pdl);
+    case 64: return launch_row_t<64>(p, st, nz, pdl);
+    case 128: return launch_row_t<128>(p, st, nz, pdl);
+    case 256: return launch_row_t<256>(p, st, nz, pdl);
+    case 512: return launch_row_t<512>(p, st, nz, pdl);
+    case 1024: return launch_row_t<1024>(p, st, nz, pdl);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -69,6 +69,7 @@ row_pass(const XParams p) {
   using C = RowCfg<LX>;
   constexpr int M = C::M, R = C::R, PL = C::PL, RW = C::RW;
   extern __shared__ float2 smem[];
+  grid_dep_sync();
   if (p.members && !p.members[blockIdx.z].active) return;   // CTA-uniform
   const int m = threadIdx.x;
   const int rl = threadIdx.y;
@@ -190,7 +191,7 @@ row_pass(const XParams p) {
 template <int LX>
 struct RowOneCfg {
   // resident CTAs per SM the register budget is sized for (RW*M = 128 threads each)
-  static constexpr int kMinBlocks = (LX <= 256) ? 4 : 2;
+  static constexpr int kMinBlocks = (LX <= 256) ? 3 : 2;
 };
 
 template <int LX>
@@ -199,6 +200,7 @@ row_pass_one(const XParams p) {
   using C = RowCfg<LX>;
   constexpr int M = C::M, R = C::R, PL = C::PL, RW = C::RW;
   extern __shared__ float2 smem[];
+  grid_dep_sync();
   if (p.members && !p.members[blockIdx.z].active) return;   // CTA-uniform
   const int m = threadIdx.x;
   const int rl = threadIdx.y;
@@ -275,6 +277,7 @@ __global__ void __launch_bounds__(256, (L <= 256) ? 4 : 2)
 line_pass(const LineParams P) {
   constexpr int M = LineCfg<L>::M, R = LineCfg<L>::R;
   extern __shared__ float2 smem[];
+  grid_dep_sync();
   if (P.members && !P.members[blockIdx.z].active) return;   // CTA-uniform
   const LineGeom<L, 1> g(P);
   float2 v[R];

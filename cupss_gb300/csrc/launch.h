@@ -5,13 +5,33 @@
 
 namespace cupssgb {
 
+// Launch configuration; pdl: programmatic stream serialization, so the kernel may
+// become resident while its predecessor in the stream drains (the step kernels wait
+// for the predecessor's completion themselves, see grid_dep_sync).
+struct LaunchCfg {
+  cudaLaunchConfig_t cfg;
+  cudaLaunchAttribute attr[1];
+  LaunchCfg(dim3 grid, dim3 block, size_t smem, cudaStream_t st, bool pdl) {
+    cfg = cudaLaunchConfig_t{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+  }
+};
+
 // Row pass over all rows (of nz batch members); picks the template by p.Lx.
-cudaError_t launch_row_pass(const XParams& p, cudaStream_t st, int nz = 1);
+cudaError_t launch_row_pass(const XParams& p, cudaStream_t st, int nz = 1, bool pdl = false);
 size_t row_pass_smem(int Lx, int n_in);
 
 // Line pass: grid.x = ceil(Lx/W) tiles, grid.y per geometry; nl = 2 for the paired
 // 3D z-turnaround.  nslots = shared-memory slots the mode needs.
-cudaError_t launch_line_pass(const LineParams& p, int nl, int nslots, dim3 grid, cudaStream_t st);
+cudaError_t launch_line_pass(const LineParams& p, int nl, int nslots, dim3 grid, cudaStream_t st,
+                             bool pdl = false);
 size_t line_pass_smem(int L, int nl, int W, int nslots);
 int line_threads(int L, int nl, int W);
 
@@ -19,11 +39,11 @@ cudaError_t launch_expand(const ExpandParams& p, cudaStream_t st);
 cudaError_t launch_compress(const CompressParams& p, cudaStream_t st);
 cudaError_t launch_mask(const MaskParams& p, cudaStream_t st);
 // Advances the step count of every active member by inc.
-cudaError_t launch_tick(MemberK* members, int n, uint32_t inc, cudaStream_t st);
+cudaError_t launch_tick(MemberK* members, int n, uint32_t inc, cudaStream_t st, bool pdl = false);
 
 // per-L launchers (one translation unit per group of sizes)
 #define CUPSSGB_DECL_LINE(L) \
-  cudaError_t launch_line_##L(const LineParams& p, int nl, size_t smem, dim3 grid, cudaStream_t st);
+  cudaError_t launch_line_##L(const LineParams& p, int nl, size_t smem, dim3 grid, cudaStream_t st, bool pdl);
 CUPSSGB_DECL_LINE(1) CUPSSGB_DECL_LINE(2) CUPSSGB_DECL_LINE(4) CUPSSGB_DECL_LINE(8)
 CUPSSGB_DECL_LINE(16) CUPSSGB_DECL_LINE(32) CUPSSGB_DECL_LINE(64) CUPSSGB_DECL_LINE(128)
 CUPSSGB_DECL_LINE(256) CUPSSGB_DECL_LINE(512) CUPSSGB_DECL_LINE(1024)

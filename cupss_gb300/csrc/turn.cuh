@@ -156,6 +156,7 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
   constexpr int R = LineCfg<L>::R;
   constexpr bool Z3 = (NL == 2);   // the paired z-line form is the 3D turnaround
   extern __shared__ float2 smem[];
+  grid_dep_sync();
   NoiseKey nk{P.key0, P.key1, P.step};
   if (P.members) {
     const MemberK mk = P.members[blockIdx.z];

@@ -762,7 +762,9 @@ void Solver::run_phase(Phase& P) {
     p.mstride = half_;
     p.mvals = mvals_d_[P.id];
   }
-  dim3 grid((Lx_ + p.W - 1) / p.W, dim_ == 3 ? std::max(sy_ / 2, 1) : 1, batch_ ? nmem_ : 1);
+  // 3D: one more tile index for the packed column kx' = 0 (see LineGeom)
+  dim3 grid((Lx_ + p.W - 1) / p.W + (dim_ == 3 ? 1 : 0), dim_ == 3 ? std::max(sy_ / 2, 1) : 1,
+            batch_ ? nmem_ : 1);
   mark_begin();
   if (use_jit_) {
     // the kernel is compiled for the tuned tile width; while tuning, one width-generic

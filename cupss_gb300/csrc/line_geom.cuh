@@ -21,10 +21,18 @@ namespace cupssgb {
 
 // WT > 0: the tile width is a compile-time constant (generated kernels), so every
 // shared-memory index below is a per-thread base plus an immediate offset.
+//
+// Paired z lines (NL = 2, the 3D turnaround): the packed column kx' = 0, whose modes
+// need two updates each (the kx = 0 and kx = sx/2 planes), gets tiles of its own so
+// that no warp mixes it with plain columns: tile index tx = ceil(Lx/W) holds, in thread
+// column w, the pair ty*W + w of column 0; the regular tiles leave column 0 out.
 template <int L, int NL, int WT = 0>
 struct LineGeom {
   static constexpr int PL = padded_len<L>();
   int W, w, m, l, kx0, kxp, lineky;
+  int pr;                // NL = 2: pair index of this thread's two lines
+  bool packed_tile;      // NL = 2: this CTA works on the packed column kx' = 0
+  bool idle;             // a packed-column CTA past the last pair (CTA-uniform)
   bool ok;
   int lofs, pstride;     // element offset of this thread's line (position 0) and stride, within a member
   size_t mbase;
@@ -40,6 +48,9 @@ struct LineGeom {
     kx0 = tx * W;
     kxp = kx0 + w;
     lineky = 0;
+    pr = ty;
+    packed_tile = false;
+    idle = false;
     bool lineok = true;
     // the paired form (NL = 2) is only used along z
     const int geo = (NL == 2) ? (int)kGeoZ3 : P.geo;
@@ -51,9 +62,19 @@ struct LineGeom {
       pstride = Lx;
     } else {
       if (NL == 2) {
-        const int pr = ty;
+        const int pairs = sy > 1 ? sy / 2 : 1;
+        if (tx * W >= Lx) {
+          packed_tile = true;
+          kx0 = 0;
+          kxp = 0;
+          pr = ty * W + w;
+          idle = ty * W >= pairs;
+          lineok = pr < pairs;
+        } else {
+          lineok = kxp != 0;
+        }
         lineky = (l == 0) ? pr : ((pr == 0) ? sy / 2 : sy - pr);
-        lineok = !(l == 1 && sy == 1);
+        lineok = lineok && !(l == 1 && sy == 1);
       } else {
         lineky = ty;
       }

@@ -165,6 +165,7 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
   }
   const Dims d = Spec::kSX ? Dims{Spec::kSX, Spec::kSY, Spec::kSZ} : dims_of(P);
   const LineGeom<L, NL, Spec::kW> g(P, d.sy, d.sx / 2);
+  if (g.idle) return;   // CTA-uniform, before any barrier
   const int m = g.m, l = g.l;
   const int slot_sz = g.slot_sz;
   const int sy = d.sy;
@@ -205,7 +206,7 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
     float2 ch[R];
 #pragma unroll
     for (int i = 0; i < R; ++i) ch[i] = make_float2(0.f, 0.f);
-    const int pl = (NL == 2 && sy > 1 && blockIdx.y != 0) ? (l ^ 1) : l;
+    const int pl = (NL == 2 && sy > 1 && g.pr != 0) ? (l ^ 1) : l;
     if (g.ok && g.kxp != 0) {
       if constexpr (Prog::kUnroll) {
         // Fourier noise of the thread's R modes, drawn in (t, t + Lt/2) pairs; ch holds
@@ -281,10 +282,10 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
     }
     // 3) inverse transform of the dealiased copy
     bool skip = !has_chan || g.kx0 > F.chan_xlimit;
-    if (Z3) {
-      // both lines of pair p >= 1 have |n_y| = p; pair 0 holds n_y = 0
-      const int pr = (int)blockIdx.y;
-      if (pr > 0 && pr > F.chan_ylimit) skip = true;
+    if (Z3 && !g.packed_tile) {
+      // both lines of pair p >= 1 have |n_y| = p; pair 0 holds n_y = 0 (the packed-column
+      // tiles hold several pairs and are never skipped: masked modes come out zero)
+      if (g.pr > 0 && g.pr > F.chan_ylimit) skip = true;
     }
     __syncthreads();   // every read of the slots is done
     if (fi + 1 < nf) prefetch_states<L>(P, P.f[fi + 1], g, smem, slot_sz);

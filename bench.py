@@ -146,17 +146,19 @@ def kernel_bytes(kind, wl):
     arr = 4.0 * N
     Lx = sx // 2
     mx = sx // 4
+    cols = (mx + 1) / Lx        # unmasked x columns (kx' <= sx/4) of a dealiased channel
     if sz > 1:
-        W = 8
+        W, Wi = 8, 16           # turnaround / y-inverse tile widths (column granularity of writes)
         fx = min(Lx, (mx // W + 1) * W) / Lx
+        fxi = min(Lx, (mx // Wi + 1) * Wi) / Lx
         fy = min(sy // 2, sy // 4 + 1) / (sy // 2)
         return {"turnaround_z": 3 * arr + fx * fy * arr,     # read G'', read/write state, write H'
-                "line_inv_y": 2 * fx * arr,                  # read H', write H (unmasked columns)
-                "row_pass": 2 * arr,                         # read H, write G'
+                "line_inv_y": fxi * fy * arr + fxi * arr,    # read H' (unmasked rows), write H
+                "row_pass": cols * arr + arr,                # read H (unmasked columns), write G'
                 "line_fwd_y": 2 * arr}[kind]                 # G' -> G''
     W = 16
     fx = min(Lx, (mx // W + 1) * W) / Lx
-    return {"turnaround_y": 3 * arr + fx * arr, "row_pass": 2 * arr}[kind]
+    return {"turnaround_y": 3 * arr + fx * arr, "row_pass": cols * arr + arr}[kind]
 
 
 def run_cpu_baseline(wl, steps_budget_s=20.0, max_steps=None, workers=None):

@@ -31,7 +31,7 @@ Solver::Solver(int sx, int sy, int sz, float dx, float dy, float dz, float dt)
   use_jit_ = !(jit && std::string(jit) == "0");
   // turnaround launch shape: tile width and resident CTAs per SM (tuning knobs)
   if (const char* w = std::getenv("CUPSSGB_TURN_W")) turn_w_ = std::atoi(w);
-  if (const char* b = std::getenv("CUPSSGB_TURN_MINB")) turn_min_blocks_ = std::max(1, std::atoi(b));
+  if (const char* b = std::getenv("CUPSSGB_TURN_WARPS")) turn_warps_ = std::max(1, std::atoi(b));
   if (const char* d = std::getenv("CUPSSGB_PDL")) pdl_ = std::string(d) != "0";
   if (!pow2(sx) || sx < 2 || sx > 2048 || !pow2(sy) || sy > 1024 || !pow2(sz) || sz > 1024)
     throw Error(kErrUnsupported,
@@ -317,6 +317,9 @@ void Solver::line_fwd_inv(int geo, int mode, const float2* in, float2* out, int 
     p.mstride = half_;
     p.members = members_d_;
   }
+  // masked inverse (dealiased channel): narrower tiles waste fewer masked columns and
+  // give more CTAs to a pass that touches only part of the grid
+  if (mode == kModeInv && xlimit < Lx_ - 1) p.W = std::min(p.W, 8);
   int tiles = (Lx_ + p.W - 1) / p.W;
   if (mode == kModeInv) tiles = std::min(tiles, xlimit / p.W + 1);   // tiles past the limit stay zero
   dim3 grid(tiles, geo == kGeoY3 ? sz_ : (geo == kGeoZ3 ? sy_ : 1), batch ? nmem_ : 1);
@@ -678,11 +681,11 @@ const std::string& Solver::turn_source(Phase& P, const LineParams& p, int L, int
     const PresK& q = p.pres[j];
     sig.insert(sig.end(), {q.q2n, q.iqx, q.iqy, q.iqz, q.invq});
   }
-  sig.push_back(turn_min_blocks_);
+  sig.push_back(turn_warps_);
   sig.push_back(batch_ ? 1 : 0);
   if (sig != P.jit_sig) {
     P.jit_sig = sig;
-    P.jit_src = jit_generate_turn(p, L, nl, turn_min_blocks_, batch_);
+    P.jit_src = jit_generate_turn(p, L, nl, turn_warps_, batch_);
   }
   return P.jit_src;
 }
@@ -698,7 +701,7 @@ std::vector<std::string> Solver::generated_sources() {
     int nslots = 0;
     bool any_chan = false;
     fill_turn(P, p, nslots, any_chan);
-    out.push_back(jit_generate_turn(p, L, nl, turn_min_blocks_, batch_));
+    out.push_back(jit_generate_turn(p, L, nl, turn_warps_, batch_));
   }
   return out;
 }

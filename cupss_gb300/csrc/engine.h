@@ -184,7 +184,7 @@ class Solver {
   bool prepared_ = false;
   bool use_jit_ = true;
   int turn_w_ = 0;            // 0: automatic tile width
-  int turn_min_blocks_ = 2;   // __launch_bounds__ min blocks of the generated turnaround
+  int turn_warps_ = 16;       // resident warps per SM the generated turnaround's registers are sized for
   bool tuning_ = false;       // autotune in progress: run the width-generic generated kernel
   bool pdl_ = true;           // step kernels use programmatic dependent launch
   long long step_ = 0;

@@ -11,6 +11,7 @@
 
 #include <nvrtc.h>
 
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <sstream>
@@ -58,7 +59,7 @@ std::string keep_expr(int s, const PresK& p, bool* never) {
 
 }  // namespace
 
-std::string jit_generate_turn(const LineParams& p, int L, int NL, int min_blocks, bool batched) {
+std::string jit_generate_turn(const LineParams& p, int L, int NL, int warps, bool batched) {
   // numerical values: the parameter block (one system) or the batch member's row
   auto pre = [&](int k) {
     return batched ? "__ldg(mv + " + std::to_string(k) + ")" : "P.pres[" + std::to_string(k) + "].pre";
@@ -67,6 +68,11 @@ std::string jit_generate_turn(const LineParams& p, int L, int NL, int min_blocks
     return batched ? "__ldg(mv + kMaxPres + " + std::to_string(fi) + ")"
                    : "P.f[" + std::to_string(fi) + "].noise_base";
   };
+  // block = (W, M, NL) threads
+  int M = 1;
+  while (4 * M * M <= L) M *= 2;   // LineCfg<L>::M = 2^floor(log2(L)/2)
+  const int threads = p.W > 0 ? p.W * M * NL : 256;
+  const int min_blocks = std::max(1, warps * 32 / threads);
   std::ostringstream o;
   o << "#include \"turn.cuh\"\n"
     << "namespace cupssgb {\n"
@@ -151,10 +157,11 @@ std::string jit_generate_turn(const LineParams& p, int L, int NL, int min_blocks
     // the phase structure and grid this kernel is specialised for
     << "struct GenSpec {\n"
     << "  static constexpr int kNF = " << p.nf << ";\n"
+    << "  static constexpr int kNProd = " << p.n_prod << ";\n"
     << "  static constexpr int kSX = " << p.sx << ", kSY = " << p.sy << ", kSZ = " << p.sz << ";\n"
     << "  static constexpr int kW = " << p.W << ";\n"
     << "};\n}  // namespace cupssgb\n"
-    << "extern \"C\" __global__ void __launch_bounds__(256, " << min_blocks
+    << "extern \"C\" __global__ void __launch_bounds__(" << threads << ", " << min_blocks
     << ") cupssgb_turn(const cupssgb::LineParams P) {\n"
     << "  cupssgb::turn_body<" << L << ", " << NL << ", cupssgb::GenProg, cupssgb::GenSpec>(P);\n}\n";
   return o.str();

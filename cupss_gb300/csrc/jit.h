@@ -12,9 +12,11 @@ namespace cupssgb {
 // program described by p (its fields, terms and prefactor exponents), the grid
 // (p.sx, p.sy, p.sz), L, NL, and, when p.W > 0, the tile width (p.W = 0: the width
 // is read from the parameter block at run time).
-// min_blocks: the minimum resident CTAs per SM requested from the compiler.
+// warps: resident warps per SM the kernel's register budget is sized for (the
+// __launch_bounds__ minimum block count is warps * 32 / threads per block; with a
+// width-generic kernel, p.W = 0, blocks of 256 threads are assumed).
 // batched: numerical values come from the batch member's row of P.mvals.
-std::string jit_generate_turn(const LineParams& p, int L, int NL, int min_blocks = 2, bool batched = false);
+std::string jit_generate_turn(const LineParams& p, int L, int NL, int warps = 16, bool batched = false);
 // Compiles (once per source text) and returns the kernel handle.  Throws Error.
 cudaKernel_t jit_kernel(const std::string& source, const char* entry);
 // Compiles for sm_103a without loading (no GPU needed); returns "" or the log.

@@ -31,11 +31,15 @@
 
 namespace cupssgb {
 
-// 8-byte asynchronous global -> shared copy (zero-filled when src_bytes is 0, in which
-// case nothing is read).
-__device__ __forceinline__ void cp_async8(float2* sdst, const float2* gsrc, int src_bytes) {
+// 32-bit shared-window address of a shared-memory pointer.
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
   unsigned sa;
-  asm volatile("{ .reg .u64 t; cvta.to.shared.u64 t, %1; cvt.u32.u64 %0, t; }" : "=r"(sa) : "l"(sdst));
+  asm("{ .reg .u64 t; cvta.to.shared.u64 t, %1; cvt.u32.u64 %0, t; }" : "=r"(sa) : "l"(p));
+  return sa;
+}
+// 8-byte asynchronous global -> shared copy to shared address sa (zero-filled when
+// src_bytes is 0, in which case nothing is read).
+__device__ __forceinline__ void cp_async8(unsigned sa, const float2* gsrc, int src_bytes) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(sa), "l"(gsrc), "r"(src_bytes) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
@@ -45,15 +49,17 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // thread's step-2 positions (zeros outside the grid).
 template <int L, class G>
 __device__ __forceinline__ void prefetch_states(const LineParams& P, const FieldK& F, const G& g, float2* smem,
-                                                int slot_sz) {
+                                                int n_prod, int slot_sz) {
   constexpr int R = LineCfg<L>::R;
+  const unsigned sbase = smem_u32(smem) + 8u * (unsigned)g.sidx(g.l, 0);
   for (int j = 0; j < F.nsrc; ++j) {
-    float2* Sj = smem + (P.n_prod + j) * slot_sz;
+    const unsigned sj = sbase + 8u * (unsigned)((n_prod + j) * slot_sz);
     const float2* st = g.at(P.state[F.src[j]]);
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       const int pos = pos_step2<L>(g.m, i);
-      cp_async8(Sj + g.sidx(g.l, pos), g.ok ? st + g.elem(pos) : st, g.ok ? 8 : 0);
+      const unsigned off = 8u * (unsigned)(g.sidx(g.l, pos) - g.sidx(g.l, 0));
+      cp_async8(sj + off, g.ok ? st + g.elem(pos) : st, g.ok ? 8 : 0);
     }
   }
   cp_async_commit();
@@ -126,6 +132,7 @@ struct InterpProg {
 // parameter offsets) and every index expression of the per-mode math folds.
 struct RtSpec {
   static constexpr int kNF = 0;
+  static constexpr int kNProd = -1;   // product channels (-1: P.n_prod)
   static constexpr int kSX = 0, kSY = 0, kSZ = 0;
   static constexpr int kW = 0;   // tile width (0: P.W)
 };
@@ -135,14 +142,15 @@ struct RtSpec {
 // or when the field has no dealiased copy).
 template <int L, bool Z3, class Prog, class G>
 __device__ __forceinline__ float2 update_mode(const LineParams& P, const Dims& d, const FieldK& F, int fi,
-                                              const G& g, int i, const float2* smem, bool has_chan, float2 xi) {
+                                              const G& g, int i, const float2* smem, int n_prod, bool has_chan,
+                                              float2 xi) {
   const int pos = pos_step2<L>(g.m, i);
   Fetch fx;
   fx.smem = smem;
   fx.slot_sz = g.slot_sz;
   fx.as = g.sidx(g.l, pos);
   fx.ap = fx.as;
-  fx.n_prod = P.n_prod;
+  fx.n_prod = n_prod;
   fx.wsel = -1;
   fx.xi = xi;
   const VPoint vp = make_vpoint(P, d, g.kxp, Z3 ? g.lineky : pos, Z3 ? pos : 0);
@@ -170,14 +178,15 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
   const int slot_sz = g.slot_sz;
   const int sy = d.sy;
   const int nf = Spec::kNF ? Spec::kNF : P.nf;
+  const int n_prod = Spec::kNProd >= 0 ? Spec::kNProd : P.n_prod;
   float2 v[R];
 
   // 0) the states the first field reads start on their way to shared memory now, and
   //    arrive while the products are transformed
-  if (nf > 0) prefetch_states<L>(P, P.f[0], g, smem, slot_sz);
+  if (nf > 0) prefetch_states<L>(P, P.f[0], g, smem, n_prod, slot_sz);
 
   // 1) forward transform of every product channel into its slot (step-2 positions)
-  for (int c = 0; c < P.n_prod; ++c) {
+  for (int c = 0; c < n_prod; ++c) {
     float2* Sl = smem + c * slot_sz;
     const float2* in = g.at(P.prod_in[c]);
 #pragma unroll
@@ -229,7 +238,7 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
           }
         }
 #pragma unroll
-        for (int i = 0; i < R; ++i) ch[i] = update_mode<L, Z3, Prog>(P, d, F, fi, g, i, smem, has_chan, ch[i]);
+        for (int i = 0; i < R; ++i) ch[i] = update_mode<L, Z3, Prog>(P, d, F, fi, g, i, smem, n_prod, has_chan, ch[i]);
       } else {
         // table-driven program: a rolled loop (its unrolled code would be very large);
         // the results go through a thread-local array into the registers
@@ -241,7 +250,7 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
             const int pos = pos_step2<L>(m, i);
             xi = Z3 ? noise_at(P, d, nk, F.fid, g.kxp, g.lineky, pos) : noise_at(P, d, nk, F.fid, g.kxp, pos, 0);
           }
-          chl[i] = update_mode<L, Z3, Prog>(P, d, F, fi, g, i, smem, has_chan, xi);
+          chl[i] = update_mode<L, Z3, Prog>(P, d, F, fi, g, i, smem, n_prod, has_chan, xi);
         }
 #pragma unroll
         for (int i = 0; i < R; ++i) ch[i] = chl[i];
@@ -262,7 +271,7 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
         fx.slot_sz = slot_sz;
         fx.as = g.sidx(l, pos);
         fx.ap = g.sidx(pl, ppos);
-        fx.n_prod = P.n_prod;
+        fx.n_prod = n_prod;
         fx.wsel = 0;
         const VPoint v0 = make_vpoint(P, d, 0, ky, kz);
         fx.xi = F.noisy ? noise_at(P, d, nk, F.fid, 0, ky, kz) : make_float2(0.f, 0.f);
@@ -288,7 +297,7 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
       if (g.pr > 0 && g.pr > F.chan_ylimit) skip = true;
     }
     __syncthreads();   // every read of the slots is done
-    if (fi + 1 < nf) prefetch_states<L>(P, P.f[fi + 1], g, smem, slot_sz);
+    if (fi + 1 < nf) prefetch_states<L>(P, P.f[fi + 1], g, smem, n_prod, slot_sz);
     if (skip) return;   // CTA-uniform: masked tile, the channel stays zero
     float2* Ts = smem + P.tslot * slot_sz;
     inv_step2<L>(ch);

@@ -38,6 +38,23 @@ WORKLOADS = {
     "ch2d-256": dict(shape=(256, 256, 1), dt=0.01, params={"a": -1.0, "b": 1.0, "k": 1.0},
                      eqs=["dt phi + q^2*(a + k*q^2)*phi = -b*q^2*phi^3"], noise=[],
                      init=(-0.1, 0.1), solve_steps=10000, steps=10000, warmup=50),
+    "ch2d-1024": dict(shape=(1024, 1024, 1), dt=0.01, params={"a": -1.0, "b": 1.0, "k": 1.0},
+                      eqs=["dt phi + q^2*(a + k*q^2)*phi = -b*q^2*phi^3"], noise=[],
+                      init=(-0.1, 0.1), solve_steps=5000, steps=2000, warmup=20),
+    # 2D model H: Cahn-Hilliard advected by the Stokes velocity of the Korteweg stress,
+    # transverse projection in Fourier space (reference examples/04_model_h)
+    "modelh-1024": dict(shape=(1024, 1024, 1), dt=0.01,
+                        params={"a": -1.0, "b": 1.0, "k": 4.0, "eta": 1.0, "T": 0.001},
+                        fields=[("phi", True), ("iqxphi", False), ("iqyphi", False), ("lapphi", False),
+                                ("vx", False), ("vy", False)],
+                        eqs=["dt phi + q^2*(a + k*q^2)*phi = -b*q^2*phi^3 - vx*iqxphi - vy*iqyphi",
+                             "iqxphi = iqx*phi", "iqyphi = iqy*phi", "lapphi = -q^2*phi",
+                             "vx*eta*q^2 = -k*iqxphi*lapphi - k*iqx^2*1/q^2*iqxphi*lapphi"
+                             " - k*iqx*iqy*1/q^2*iqyphi*lapphi",
+                             "vy*eta*q^2 = -k*iqyphi*lapphi - k*iqy^2*1/q^2*iqyphi*lapphi"
+                             " - k*iqx*iqy*1/q^2*iqxphi*lapphi"],
+                        noise=[("phi", "2*T")], init=(-0.1, 0.1), solve_steps=5000, steps=1000, warmup=10,
+                        B_alg=80.0),
 }
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM = 6800.0
@@ -103,7 +120,8 @@ def make_evolver(wl, seed=42):
     import cupss_gb300 as c
     sx, sy, sz = wl["shape"]
     e = c.Evolver(True, sx, sy, sz, 1.0, 1.0, 1.0, dt=wl["dt"], write_every=10 ** 9)
-    e.createField("phi", True)
+    for nm, dyn in wl.get("fields", [("phi", True)]):
+        e.createField(nm, dyn)
     for k, v in wl["params"].items():
         e.addParameter(k, v)
     for q in wl["eqs"]:
@@ -137,10 +155,13 @@ class _SolverView:
 
 
 def kernel_bytes(kind, wl):
-    """Algorithmic bytes per launch of each kernel of the 3D/2D Cahn-Hilliard step.
+    """Algorithmic bytes per launch of each kernel of the 3D/2D Cahn-Hilliard step
+    (None for the multi-field workloads, which are reported against their step model).
     Spectral arrays are packed half spectra: 8 B per complex = 4 B per grid point.
     Dealiased channels (order 3, |n| <= N/4) are written only where unmasked, at the
     engine's tile granularity (W columns x line pairs)."""
+    if "fields" in wl:
+        return None
     sx, sy, sz = wl["shape"]
     N = sx * sy * sz
     arr = 4.0 * N
@@ -176,7 +197,8 @@ def run_cpu_baseline(wl, steps_budget_s=20.0, max_steps=None, workers=None):
 
     def build(shape):
         s = System()
-        s.create_field("phi", True)
+        for nm, dyn in wl.get("fields", [("phi", True)]):
+            s.create_field(nm, dyn)
         for k, v in wl["params"].items():
             s.add_parameter(k, v)
         for q in wl["eqs"]:
@@ -536,8 +558,11 @@ def main():
         dist.init_process_group("gloo")
     sx, sy, sz = wl["shape"]
     N = sx * sy * sz
-    cfg = {"workload": "%s: %dx%dx%d Cahn-Hilliard%s, dt=%g, FP32" % (
-        args.workload, sx, sy, sz, " + conserved noise T=0.01" if wl["noise"] else "", wl["dt"]),
+    system = "model H (6 fields)" if "fields" in wl else "Cahn-Hilliard"
+    noise = ""
+    if wl["noise"]:
+        noise = " + conserved noise T=0.01" if "q^2" in wl["noise"][0][1] else " + noise T=%g" % wl["params"]["T"]
+    cfg = {"workload": "%s: %dx%dx%d %s%s, dt=%g, FP32" % (args.workload, sx, sy, sz, system, noise, wl["dt"]),
         "grid": [sx, sy, sz], "equation": wl["eqs"][0], "noise": wl["noise"][0][1] if wl["noise"] else None,
         "full_solve_steps": wl["solve_steps"],
         "l2": "working set (state x2, dealiased copies, product spectra) larger than the 126 MB L2",
@@ -587,15 +612,16 @@ def main():
         avg = v["ms"] / v["launches"]
         byts = kernel_bytes(kind, wl)
         per[kind] = {"launches": v["launches"], "avg_us": 1e3 * avg, "share": None,
-                     "alg_bytes": byts, "GBps": byts / (avg * 1e-3) / 1e9}
+                     "alg_bytes": byts, "GBps": None if byts is None else byts / (avg * 1e-3) / 1e9}
     tot = sum(v["ms"] for v in rep.values())
     for kind in per:
         per[kind]["share"] = rep[kind]["ms"] / tot
     dom = max(per, key=lambda k: rep[k]["ms"])
     d = per[dom]
-    B_alg = 24.0
+    B_alg = wl.get("B_alg", 24.0)
     roof = {"bound": "hbm", "kernel": dom, "achieved": d["GBps"], "peak": peak, "unit": "GB/s",
-            "frac": d["GBps"] / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+            "frac": None if d["GBps"] is None else d["GBps"] / peak,
+            "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
             "traffic": None, "alg_bytes_per_launch": d["alg_bytes"], "avg_launch_us": d["avg_us"],
             "kernels": per,
             "step_model": {"B_alg_per_pt_step": B_alg,

@@ -322,7 +322,7 @@ void Solver::line_fwd_inv(int geo, int mode, const float2* in, float2* out, int 
   if (mode == kModeInv && xlimit < Lx_ - 1) p.W = std::min(p.W, 8);
   int tiles = (Lx_ + p.W - 1) / p.W;
   if (mode == kModeInv) tiles = std::min(tiles, xlimit / p.W + 1);   // tiles past the limit stay zero
-  dim3 grid(tiles, geo == kGeoY3 ? sz_ : (geo == kGeoZ3 ? sy_ : 1), batch ? nmem_ : 1);
+  dim3 grid(tiles, geo == kGeoY3 ? sz_ : (geo == kGeoZ3 ? sy_ : 1), batch ? mspan_ : 1);
   check(launch_line_pass(p, 1, 1, grid, stream_, pdl), "line pass");
   ++launches_;
 }
@@ -737,7 +737,7 @@ void Solver::run_phase(Phase& P) {
     x.members = members_d_;
     if (batch_) x.mstride = half_;
     mark_begin();
-    check(launch_row_pass(x, stream_, batch_ ? nmem_ : 1, pdl_), "row pass");
+    check(launch_row_pass(x, stream_, batch_ ? mspan_ : 1, pdl_), "row pass");
     mark_end("row_pass");
     ++launches_;
     if (dim_ == 3) {
@@ -767,7 +767,7 @@ void Solver::run_phase(Phase& P) {
   }
   // 3D: one more tile index for the packed column kx' = 0 (see LineGeom)
   dim3 grid((Lx_ + p.W - 1) / p.W + (dim_ == 3 ? 1 : 0), dim_ == 3 ? std::max(sy_ / 2, 1) : 1,
-            batch_ ? nmem_ : 1);
+            batch_ ? mspan_ : 1);
   mark_begin();
   if (use_jit_) {
     // the kernel is compiled for the tuned tile width; while tuning, one width-generic

@@ -192,6 +192,7 @@ class Solver {
   size_t dev_bytes_ = 0;
   // batches
   int nmem_ = 1;
+  int mspan_ = 1;   // members covered by step launches: 1 + the last active slot
   bool batch_ = false;
   size_t half_ = 0;                              // elements of one member's spectrum
   std::vector<std::vector<HostField>> mfields_;  // per member (values only differ)

@@ -22,6 +22,7 @@ void Solver::set_members(int n) {
   if (prepared_) throw Error(kErrState, "set_members after prepare");
   if (n < 1 || n > 65535) throw Error(kErrInvalid, "a batch holds 1 to 65535 members");
   nmem_ = n;
+  mspan_ = n;
   batch_ = true;
   mfields_.clear();
   members_h_.assign(n, MemberK{0u, 0u, 0u, 1u});
@@ -102,6 +103,18 @@ void Solver::set_member_active(int m, bool on) {
     check(cudaMemcpyAsync(&members_d_[m].active, &members_h_[m].active, sizeof(uint32_t), cudaMemcpyHostToDevice,
                           stream_),
           "member flag upload");
+  // step launches cover members [0, last active]: a sparsely filled pool does not launch
+  // (and retire) the CTAs of its empty slots beyond that
+  int span = 1;
+  for (int k = nmem_ - 1; k >= 0; --k)
+    if (members_h_[k].active) {
+      span = k + 1;
+      break;
+    }
+  if (span != mspan_) {
+    mspan_ = span;
+    invalidate_graphs();
+  }
 }
 
 void Solver::reset_member(int m) {
@@ -182,6 +195,8 @@ void Solver::autotune() {
   check(cudaEventCreate(&b), "cudaEventCreate");
   const long long l0 = launches_;
   tuning_ = true;
+  const int span0 = mspan_;
+  mspan_ = nmem_;
   // time with every slot active (a pool may be prepared with all slots free)
   std::vector<MemberK> all = members_h_;
   for (MemberK& k : all) k.active = 1u;
@@ -224,6 +239,7 @@ void Solver::autotune() {
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   tuning_ = false;
+  mspan_ = span0;
   launches_ = l0;
   check(cudaMemcpyAsync(members_d_, members_h_.data(), members_h_.size() * sizeof(MemberK), cudaMemcpyHostToDevice,
                         stream_),

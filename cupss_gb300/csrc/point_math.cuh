@@ -130,6 +130,15 @@ __device__ __forceinline__ int line_axis_len(const Dims& d) {
   return d.sz > 1 ? d.sz : (d.sy > 1 ? d.sy : 1);
 }
 
+// Both modes (t, t + Lt/2) of a folded pair from its counter lin (see noise_pair).
+__device__ __forceinline__ void noise_pair_lin(const LineParams& P, const NoiseKey& nk, int fid, uint32_t lin,
+                                               float2& lo, float2& hi) {
+  float g1, g2, g3, g4;
+  philox_normal4(lin, nk.step, (uint32_t)fid, nk.key0, nk.key1, g1, g2, g3, g4);
+  lo = make_float2(P.sqrtHalfN * g1, P.sqrtHalfN * g2);
+  hi = make_float2(P.sqrtHalfN * g3, P.sqrtHalfN * g4);
+}
+
 // Both modes (t, t + Lt/2) of a folded pair, t < Lt/2, 0 < kx < sx/2.
 __device__ __forceinline__ void noise_pair(const LineParams& P, const Dims& d, const NoiseKey& nk, int fid, int kx,
                                            int ky, int kz, float2& lo, float2& hi) {
@@ -174,6 +183,55 @@ __device__ __forceinline__ float2 noise_at(const LineParams& P, const Dims& d, c
   return make_float2(P.sqrtHalfN * g1, conj ? -P.sqrtHalfN * g2 : P.sqrtHalfN * g2);
 }
 
+// Per-thread constants of the plain modes (kx' > 0) of one line along the last axis (z
+// in 3D, y in 2D): every coordinate of the mode but the one along the line, which is
+// m + C for register index i of thread m (C = pos_step2<L>(0, i) becomes a compile-time
+// constant once the register loop unrolls, so the wrap, Nyquist and mask tests along the
+// line reduce to one comparison of m with a constant).
+struct LinePre {
+  VPoint base;        // the fixed axes; the line axis is filled in per mode
+  float fm;           // (float)m
+  uint32_t lin0;      // noise counter of line position m
+  uint32_t lin_step;  // noise counter increment per line position
+};
+
+template <bool Z3>
+__device__ __forceinline__ LinePre line_pre(const LineParams& P, const Dims& d, int kx, int ky, int m) {
+  LinePre lp;
+  lp.base = make_vpoint(P, d, kx, Z3 ? ky : 0, 0);
+  lp.fm = (float)m;
+  if (Z3) {
+    lp.lin0 = ((uint32_t)m * d.sy + ky) * d.sx + kx;
+    lp.lin_step = (uint32_t)d.sy * d.sx;
+  } else {
+    lp.lin0 = (uint32_t)m * d.sx + kx;
+    lp.lin_step = (uint32_t)d.sx;
+  }
+  return lp;
+}
+
+// The mode at line position m + C; the same values as make_vpoint (q is the exact
+// float of the wrapped integer index times the step, as in q_of).
+template <int L, bool Z3>
+__device__ __forceinline__ VPoint line_vpoint(const LineParams& P, const LinePre& lp, int m, int C) {
+  VPoint vp = lp.base;
+  const bool wrap = (L > 1) && (C >= L / 2);
+  const float q = (lp.fm + (float)(C - (wrap ? L : 0))) * (Z3 ? P.stepqz : P.stepqy);
+  const bool ny = (L > 1) && (m == L / 2 - C);
+  if (Z3) {
+    vp.kz = m + C;
+    vp.qz = q;
+    vp.nyz = ny;
+  } else {
+    vp.ky = m + C;
+    vp.qy = q;
+    vp.nyy = ny;
+  }
+  vp.origin = (vp.kx == 0 && vp.ky == 0 && vp.kz == 0);
+  vp.q2 = vp.qx * vp.qx + vp.qy * vp.qy + vp.qz * vp.qz;
+  return vp;
+}
+
 // dealias_k mask (src/field_kernels.cu:229-256): keep a mode iff |n| <= N/(order+1)
 // on every axis, n = k or k - N for k > N/2.  The three limits are per-field
 // constants (FieldK::chan_xlimit / chan_ylimit / chan_zlimit).
@@ -184,6 +242,13 @@ __device__ __forceinline__ bool keep_axis(int k, int n, int lim) {
 __device__ __forceinline__ bool keep_point(const Dims& d, const VPoint& vp, const FieldK& F) {
   return keep_axis(vp.kx, d.sx, F.chan_xlimit) && keep_axis(vp.ky, d.sy, F.chan_ylimit) &&
          keep_axis(vp.kz, d.sz, F.chan_zlimit);
+}
+// keep_axis along a line of length L at position m + C (see LinePre): positions below
+// L/2 are m + C, the others L - m - C.
+template <int L>
+__device__ __forceinline__ bool keep_line(int m, int C, int lim) {
+  if (L == 1) return true;
+  return (C < L / 2) ? (m <= lim - C) : (m >= L - C - lim);
 }
 
 // Unpacks component `which` (0: kx = 0 plane, 1: kx = sx/2 plane) of a packed value.

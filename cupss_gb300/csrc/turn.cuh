@@ -140,11 +140,13 @@ struct RtSpec {
 // One plain (kx' > 0) mode: register index i of the thread's step-2 positions.  Writes
 // the new state and returns the dealiased, 1/N-scaled copy of the mode (zero when masked
 // or when the field has no dealiased copy).
+// keep_fixed: the dealias test of the axes other than the line axis (per thread and field).
 template <int L, bool Z3, class Prog, class G>
-__device__ __forceinline__ float2 update_mode(const LineParams& P, const Dims& d, const FieldK& F, int fi,
+__device__ __forceinline__ float2 update_mode(const LineParams& P, const LinePre& lp, const FieldK& F, int fi,
                                               const G& g, int i, const float2* smem, int n_prod, bool has_chan,
-                                              float2 xi) {
-  const int pos = pos_step2<L>(g.m, i);
+                                              bool keep_fixed, float2 xi) {
+  const int C = pos_step2<L>(0, i);
+  const int pos = g.m + C;
   Fetch fx;
   fx.smem = smem;
   fx.slot_sz = g.slot_sz;
@@ -153,10 +155,11 @@ __device__ __forceinline__ float2 update_mode(const LineParams& P, const Dims& d
   fx.n_prod = n_prod;
   fx.wsel = -1;
   fx.xi = xi;
-  const VPoint vp = make_vpoint(P, d, g.kxp, Z3 ? g.lineky : pos, Z3 ? pos : 0);
+  const VPoint vp = line_vpoint<L, Z3>(P, lp, g.m, C);
   const float2 z = Prog::eval(P, fi, vp, fx);
   g.at(F.next)[g.elem(pos)] = z;
-  return (has_chan && keep_point(d, vp, F)) ? c_scale(z, P.invN) : make_float2(0.f, 0.f);
+  const bool keep = keep_fixed && keep_line<L>(g.m, C, Z3 ? F.chan_zlimit : F.chan_ylimit);
+  return (has_chan && keep) ? c_scale(z, P.invN) : make_float2(0.f, 0.f);
 }
 
 template <int L, int NL, class Prog, class Spec = RtSpec>
@@ -217,6 +220,9 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
     for (int i = 0; i < R; ++i) ch[i] = make_float2(0.f, 0.f);
     const int pl = (NL == 2 && sy > 1 && g.pr != 0) ? (l ^ 1) : l;
     if (g.ok && g.kxp != 0) {
+      const LinePre lp = line_pre<Z3>(P, d, g.kxp, g.lineky, m);
+      const bool keep_fixed = keep_axis(g.kxp, d.sx, F.chan_xlimit) &&
+                              (Z3 ? keep_axis(g.lineky, d.sy, F.chan_ylimit) : keep_axis(0, d.sz, F.chan_zlimit));
       if constexpr (Prog::kUnroll) {
         // Fourier noise of the thread's R modes, drawn in (t, t + Lt/2) pairs; ch holds
         // the noise until the update of its mode replaces it
@@ -228,17 +234,16 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
             const int kp = (Mx >= 2) ? (i % Mx) : (i / Mx);
             const bool lower = (L == 1) || ((Mx >= 2) ? (kp < Mx / 2) : (kp < R / 2));
             if (lower) {
-              const int pos = pos_step2<L>(m, i);
               float2 lo, hi;
-              if (Z3) noise_pair(P, d, nk, F.fid, g.kxp, g.lineky, pos, lo, hi);
-              else noise_pair(P, d, nk, F.fid, g.kxp, pos, 0, lo, hi);
+              noise_pair_lin(P, nk, F.fid, lp.lin0 + (uint32_t)pos_step2<L>(0, i) * lp.lin_step, lo, hi);
               ch[i] = lo;
               if (L > 1) ch[i + HALF] = hi;
             }
           }
         }
 #pragma unroll
-        for (int i = 0; i < R; ++i) ch[i] = update_mode<L, Z3, Prog>(P, d, F, fi, g, i, smem, n_prod, has_chan, ch[i]);
+        for (int i = 0; i < R; ++i)
+          ch[i] = update_mode<L, Z3, Prog>(P, lp, F, fi, g, i, smem, n_prod, has_chan, keep_fixed, ch[i]);
       } else {
         // table-driven program: a rolled loop (its unrolled code would be very large);
         // the results go through a thread-local array into the registers
@@ -250,7 +255,7 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
             const int pos = pos_step2<L>(m, i);
             xi = Z3 ? noise_at(P, d, nk, F.fid, g.kxp, g.lineky, pos) : noise_at(P, d, nk, F.fid, g.kxp, pos, 0);
           }
-          chl[i] = update_mode<L, Z3, Prog>(P, d, F, fi, g, i, smem, n_prod, has_chan, xi);
+          chl[i] = update_mode<L, Z3, Prog>(P, lp, F, fi, g, i, smem, n_prod, has_chan, keep_fixed, xi);
         }
 #pragma unroll
         for (int i = 0; i < R; ++i) ch[i] = chl[i];

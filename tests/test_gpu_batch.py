@@ -191,3 +191,53 @@ def test_batch_solver_inactive_and_reset():
     assert s.member_step(1) == 20 and s.member_step(2) == 40
     s.close()
     s2.close()
+
+
+def test_batch_trailing_inactive_members_are_not_launched():
+    """Launches cover members up to the last active one: deactivating the trailing
+    members shrinks the launches (and their graphs), reactivating one regrows them, and
+    every member's result stays that of its own solve."""
+    import cupss_gb300 as c
+    from cupss_gb300.capi import Pres
+
+    def system(s):
+        f = s.add_field(True)
+        s.set_implicit(f, [Pres(-1.0, 1, 0, 0, 0, 0)])
+        s.set_noise(f, Pres(0.02, 0, 0, 0, 0, 0))
+        return f
+
+    s = c.Solver(32, 16, 8, dt=0.01)
+    f = system(s)
+    s.set_members(4)
+    for m in range(4):
+        s.set_member_seed(m, 100 + m)
+    s.prepare()
+    init = splitmix64_uniform(32 * 16 * 8, 11, -1, 1).reshape(8, 16, 32)
+    for m in range(4):
+        s.set_real_member(f, m, init)
+    s.set_member_active(2, False)
+    s.set_member_active(3, False)
+    held = [s.get_real_member(f, m) for m in (2, 3)]
+    s.advance(32)   # two graph replays over members 0 and 1
+    assert [s.member_step(m) for m in range(4)] == [32, 32, 0, 0]
+    assert np.array_equal(s.get_real_member(f, 2), held[0])
+    assert np.array_equal(s.get_real_member(f, 3), held[1])
+    s.set_member_active(3, True)
+    s.advance(16)
+    assert [s.member_step(m) for m in range(4)] == [48, 48, 0, 16]
+    assert np.array_equal(s.get_real_member(f, 2), held[0])
+
+    def single(seed, nsteps):
+        s2 = c.Solver(32, 16, 8, dt=0.01)
+        g = system(s2)
+        s2.set_seed(seed)
+        s2.prepare()
+        s2.set_real(g, init)
+        s2.advance(nsteps)
+        out = s2.get_real(g)
+        s2.close()
+        return out
+
+    assert rel(s.get_real_member(f, 0), single(100, 48)) < 1e-6
+    assert rel(s.get_real_member(f, 3), single(103, 16)) < 1e-6
+    s.close()

@@ -196,10 +196,15 @@ void Solver::autotune() {
   const long long l0 = launches_;
   tuning_ = true;
   const int span0 = mspan_;
-  mspan_ = nmem_;
-  // time with every slot active (a pool may be prepared with all slots free)
+  // time the members as they are (an ensemble: all of them); a pool prepared with every
+  // slot free is timed with one member, the load a server pool mostly runs at
   std::vector<MemberK> all = members_h_;
-  for (MemberK& k : all) k.active = 1u;
+  bool any = false;
+  for (const MemberK& k : all) any = any || k.active != 0u;
+  if (!any) {
+    all[0].active = 1u;
+    mspan_ = 1;
+  }
   check(cudaMemcpyAsync(members_d_, all.data(), all.size() * sizeof(MemberK), cudaMemcpyHostToDevice, stream_),
         "member upload");
   for (Phase& P : phases_) {

@@ -50,6 +50,44 @@ __device__ __forceinline__ float2 r2c_post(float2 zk, float2 zm, int k, int sx, 
   return c_add(e, c_mul(tw_load(tw, sx, k), o));
 }
 
+// The same two steps with the twiddle w = W_sx^k given.
+__device__ __forceinline__ float2 c2r_pre_w(float2 a, float2 bm, int k, float2 w) {
+  if (k == 0) return make_float2(a.x + a.y, a.x - a.y);
+  const float2 b = c_conj(bm);
+  return c_add(c_add(a, b), c_muli(c_mulc(c_sub(a, b), w)));
+}
+__device__ __forceinline__ float2 r2c_post_w(float2 zk, float2 zm, int k, float2 w) {
+  if (k == 0) return make_float2(zk.x + zk.y, zk.x - zk.y);
+  const float2 zc = c_conj(zm);
+  const float2 e = c_scale(c_add(zk, zc), 0.5f);
+  const float2 o = c_scale(c_mulmi(c_sub(zk, zc)), 0.5f);
+  return c_add(e, c_mul(w, o));
+}
+
+// Compile-time loop: f(ic<0>{}), ..., f(ic<N-1>{}) (each index usable as a template argument).
+template <int N>
+struct ic {
+  static constexpr int value = N;
+};
+template <class F, int... I>
+__device__ __forceinline__ void static_for(iseq<I...>, F&& f) {
+  (f(ic<I>{}), ...);
+}
+
+// Twiddle W_sx^k of register I of thread m in the step-2 layout of a packed row
+// (k = m + M (j + J k'), I = j M + k'), from W_sx^m: W_sx^k = W_sx^m W_{2R}^{j + J k'}, the
+// second factor a compile-time constant (sx = 2 R M).  One table load per thread instead
+// of one per register; usable while 2R <= 32 (the compile-time twiddle table).
+template <int LX>
+struct RowTwSplit {
+  static constexpr bool value = (2 * LineCfg<LX>::R <= 32) && (LineCfg<LX>::M > 1);
+};
+template <int LX, int I>
+__device__ __forceinline__ float2 row_twiddle(float2 wm) {
+  constexpr int M = LineCfg<LX>::M, R = LineCfg<LX>::R, J = R / M;
+  return tw_const<2 * R, I / M + J * (I % M), false>(wm);
+}
+
 template <int LX>
 struct RowCfg {
   static constexpr int M = LineCfg<LX>::M;
@@ -191,7 +229,7 @@ row_pass(const XParams p) {
 template <int LX>
 struct RowOneCfg {
   // resident CTAs per SM the register budget is sized for (RW*M = 128 threads each)
-  static constexpr int kMinBlocks = (LX <= 256) ? 3 : 2;
+  static constexpr int kMinBlocks = (LX <= 256) ? 4 : 2;
 };
 
 template <int LX>
@@ -219,10 +257,19 @@ row_pass_one(const XParams p) {
     T[pad_pos<LX>(k)] = v[i];
   }
   __syncthreads();
+  if constexpr (RowTwSplit<LX>::value) {
+    const float2 wm = tw_load(p.tw, sx, m);
+    static_for(make_iseq<R>{}, [&](auto I) {
+      constexpr int i = decltype(I)::value;
+      const int k = pos_step2<LX>(m, i);
+      v[i] = c2r_pre_w(v[i], T[pad_pos<LX>((LX - k) & (LX - 1))], k, row_twiddle<LX, i>(wm));
+    });
+  } else {
 #pragma unroll
-  for (int i = 0; i < R; ++i) {
-    const int k = pos_step2<LX>(m, i);
-    v[i] = c2r_pre(v[i], T[pad_pos<LX>((LX - k) & (LX - 1))], k, sx, p.tw);
+    for (int i = 0; i < R; ++i) {
+      const int k = pos_step2<LX>(m, i);
+      v[i] = c2r_pre(v[i], T[pad_pos<LX>((LX - k) & (LX - 1))], k, sx, p.tw);
+    }
   }
   inv_step2<LX>(v);
   __syncthreads();
@@ -257,12 +304,22 @@ row_pass_one(const XParams p) {
   for (int i = 0; i < R; ++i) T[pad_pos<LX>(pos_step2<LX>(m, i))] = v[i];
   __syncthreads();
   float2* out = reinterpret_cast<float2*>(p.out[0]) + rowoff;
+  if constexpr (RowTwSplit<LX>::value) {
+    const float2 wm = tw_load(p.tw, sx, m);
+    static_for(make_iseq<R>{}, [&](auto I) {
+      constexpr int i = decltype(I)::value;
+      const int k = pos_step2<LX>(m, i);
+      const float2 x = r2c_post_w(v[i], T[pad_pos<LX>((LX - k) & (LX - 1))], k, row_twiddle<LX, i>(wm));
+      if (live) out[k] = x;
+    });
+  } else {
 #pragma unroll
-  for (int i = 0; i < R; ++i) {
-    const int k = pos_step2<LX>(m, i);
-    const float2 zm = T[pad_pos<LX>((LX - k) & (LX - 1))];
-    const float2 x = r2c_post(v[i], zm, k, sx, p.tw);
-    if (live) out[k] = x;
+    for (int i = 0; i < R; ++i) {
+      const int k = pos_step2<LX>(m, i);
+      const float2 zm = T[pad_pos<LX>((LX - k) & (LX - 1))];
+      const float2 x = r2c_post(v[i], zm, k, sx, p.tw);
+      if (live) out[k] = x;
+    }
   }
 }
 

@@ -12,6 +12,7 @@
 #include <nvrtc.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <sstream>
@@ -73,6 +74,10 @@ std::string jit_generate_turn(const LineParams& p, int L, int NL, int warps, boo
   while (4 * M * M <= L) M *= 2;   // LineCfg<L>::M = 2^floor(log2(L)/2)
   const int threads = p.W > 0 ? p.W * M * NL : 256;
   const int min_blocks = std::max(1, warps * 32 / threads);
+  // overlap of the first field's noise with the first product's loads: for spectra that
+  // do not stay in the L2 (64 MB and more per array); CUPSSGB_EARLY_NOISE=0/1 overrides
+  bool early_noise = (double)p.Lx * p.sy * p.sz * 8.0 >= 64.0 * 1024 * 1024;
+  if (const char* e = std::getenv("CUPSSGB_EARLY_NOISE")) early_noise = std::string(e) == "1";
   std::ostringstream o;
   o << "#include \"turn.cuh\"\n"
     << "namespace cupssgb {\n"
@@ -160,6 +165,7 @@ std::string jit_generate_turn(const LineParams& p, int L, int NL, int warps, boo
     << "  static constexpr int kNProd = " << p.n_prod << ";\n"
     << "  static constexpr int kSX = " << p.sx << ", kSY = " << p.sy << ", kSZ = " << p.sz << ";\n"
     << "  static constexpr int kW = " << p.W << ";\n"
+    << "  static constexpr bool kEarlyNoise = " << (early_noise ? "true" : "false") << ";\n"
     << "};\n}  // namespace cupssgb\n"
     << "extern \"C\" __global__ void __launch_bounds__(" << threads << ", " << min_blocks
     << ") cupssgb_turn(const cupssgb::LineParams P) {\n"

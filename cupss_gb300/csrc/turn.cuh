@@ -135,11 +135,36 @@ struct RtSpec {
   static constexpr int kNProd = -1;   // product channels (-1: P.n_prod)
   static constexpr int kSX = 0, kSY = 0, kSZ = 0;
   static constexpr int kW = 0;   // tile width (0: P.W)
+  // draw the first field's noise while the first product's loads are in flight (pays off
+  // when those loads come from HBM; for grids whose arrays stay in L2 it only delays the
+  // transform)
+  static constexpr bool kEarlyNoise = false;
 };
 
 // One plain (kx' > 0) mode: register index i of the thread's step-2 positions.  Writes
 // the new state and returns the dealiased, 1/N-scaled copy of the mode (zero when masked
 // or when the field has no dealiased copy).
+// Fourier noise of a thread's R plain modes of one line, drawn in (t, t + Lt/2) pairs
+// (one generator call per pair).
+template <int L>
+__device__ __forceinline__ void draw_line_noise(const LineParams& P, const NoiseKey& nk, int fid, const LinePre& lp,
+                                                float2 (&xi)[LineCfg<L>::R]) {
+  constexpr int R = LineCfg<L>::R;
+  constexpr int Mx = LineCfg<L>::M;
+  constexpr int HALF = (Mx >= 2) ? Mx / 2 : R / 2;   // register offset of t + L/2
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int kp = (Mx >= 2) ? (i % Mx) : (i / Mx);
+    const bool lower = (L == 1) || ((Mx >= 2) ? (kp < Mx / 2) : (kp < R / 2));
+    if (lower) {
+      float2 lo, hi;
+      noise_pair_lin(P, nk, fid, lp.lin0 + (uint32_t)pos_step2<L>(0, i) * lp.lin_step, lo, hi);
+      xi[i] = lo;
+      if (L > 1) xi[i + HALF] = hi;
+    }
+  }
+}
+
 // keep_fixed: the dealias test of the axes other than the line axis (per thread and field).
 template <int L, bool Z3, class Prog, class G>
 __device__ __forceinline__ float2 update_mode(const LineParams& P, const LinePre& lp, const FieldK& F, int fi,
@@ -188,12 +213,26 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
   //    arrive while the products are transformed
   if (nf > 0) prefetch_states<L>(P, P.f[0], g, smem, n_prod, slot_sz);
 
-  // 1) forward transform of every product channel into its slot (step-2 positions)
-  for (int c = 0; c < n_prod; ++c) {
-    float2* Sl = smem + c * slot_sz;
+  // 1) forward transform of every product channel into its slot (step-2 positions).
+  //    The first field's Fourier noise depends on no data: with a generated program it is
+  //    drawn while the first product's loads are in flight.
+  const bool plain = g.ok && g.kxp != 0;
+  float2 xi0[R];
+#pragma unroll
+  for (int i = 0; i < R; ++i) xi0[i] = make_float2(0.f, 0.f);
+  auto load_product = [&](int c) {
     const float2* in = g.at(P.prod_in[c]);
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = g.ok ? in[g.elem(pos_step1<L>(m, r))] : make_float2(0.f, 0.f);
+  };
+  if (n_prod > 0) load_product(0);
+  if constexpr (Prog::kUnroll && Spec::kEarlyNoise) {
+    if (nf > 0 && plain && P.f[0].noisy)
+      draw_line_noise<L>(P, nk, P.f[0].fid, line_pre<Z3>(P, d, g.kxp, g.lineky, m), xi0);
+  }
+  for (int c = 0; c < n_prod; ++c) {
+    float2* Sl = smem + c * slot_sz;
+    if (c > 0) load_product(c);
     fwd_step1<L>(v, m, P.tw);
 #pragma unroll
     for (int s = 0; s < R; ++s) Sl[g.sidx(l, pos_t1<L>(m, s))] = v[s];
@@ -224,22 +263,13 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
       const bool keep_fixed = keep_axis(g.kxp, d.sx, F.chan_xlimit) &&
                               (Z3 ? keep_axis(g.lineky, d.sy, F.chan_ylimit) : keep_axis(0, d.sz, F.chan_zlimit));
       if constexpr (Prog::kUnroll) {
-        // Fourier noise of the thread's R modes, drawn in (t, t + Lt/2) pairs; ch holds
-        // the noise until the update of its mode replaces it
-        if (F.noisy) {
-          constexpr int Mx = LineCfg<L>::M;
-          constexpr int HALF = (Mx >= 2) ? Mx / 2 : R / 2;   // register offset of t + L/2
+        // Fourier noise of the thread's R modes; ch holds the noise until the update of
+        // its mode replaces it (the first field's was drawn during the product loads)
+        if (Spec::kEarlyNoise && fi == 0) {
 #pragma unroll
-          for (int i = 0; i < R; ++i) {
-            const int kp = (Mx >= 2) ? (i % Mx) : (i / Mx);
-            const bool lower = (L == 1) || ((Mx >= 2) ? (kp < Mx / 2) : (kp < R / 2));
-            if (lower) {
-              float2 lo, hi;
-              noise_pair_lin(P, nk, F.fid, lp.lin0 + (uint32_t)pos_step2<L>(0, i) * lp.lin_step, lo, hi);
-              ch[i] = lo;
-              if (L > 1) ch[i + HALF] = hi;
-            }
-          }
+          for (int i = 0; i < R; ++i) ch[i] = xi0[i];
+        } else if (F.noisy) {
+          draw_line_noise<L>(P, nk, F.fid, lp, ch);
         }
 #pragma unroll
         for (int i = 0; i < R; ++i)

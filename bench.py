@@ -499,6 +499,10 @@ def bench_served(args):
             "speedup_vs_plain": (done - reqs[0]["arrival"]) / makespan,
             "accuracy": {"requests_equal_to_plain": int(agree), "tolerance": "rel L2 1e-6"},
             "server_stats": stats, "warm_s": warm_s, "clocks": clk}
+    # the requests that finished last: (system, grid, steps, admitted after, latency) in s
+    order = np.argsort([t[2] for t in times])[::-1][:6]
+    line["last_finished"] = [[reqs[i]["system"], list(reqs[i]["shape"]), int(reqs[i]["steps"]),
+                              round(times[i][1] - times[i][0], 3), round(float(lat[i]), 3)] for i in order]
     print(json.dumps(line), flush=True)
 
 

@@ -82,7 +82,7 @@ CG_HD float2 c_scale(float2 a, float s) { return make_float2(a.x * s, a.y * s); 
 CG_HD float2 c_muli(float2 a) { return make_float2(-a.y, a.x); }    // i * a
 CG_HD float2 c_mulmi(float2 a) { return make_float2(a.y, -a.x); }   // -i * a
 
-// Multiply by W_N^K (forward, W = exp(-2 pi i/N)) or its conjugate (INV), N <= 32.
+// Multiply by W_N^K (forward, W = exp(-2 pi i/N)) or its conjugate (INV), N <= 64.
 template <int N, int K, bool INV>
 CG_HD float2 tw_const(float2 a) {
   constexpr int k = K % N;
@@ -95,9 +95,9 @@ CG_HD float2 tw_const(float2 a) {
   } else if constexpr (4 * k == 3 * N) {
     return INV ? c_mulmi(a) : c_muli(a);
   } else {
-    constexpr int j = k * (32 / N);
-    constexpr float wr = kTw32Re[j];
-    constexpr float wi = INV ? -kTw32Im[j] : kTw32Im[j];
+    constexpr int j = k * (64 / N);
+    constexpr float wr = kTw64Re[j];
+    constexpr float wi = INV ? -kTw64Im[j] : kTw64Im[j];
     return c_mul(a, make_float2(wr, wi));
   }
 }

@@ -1,7 +1,9 @@
-"""Writes twiddle32.h: exp(-2*pi*i*j/32), j in [0,32), as exact float hex literals.
+"""Writes twiddle32.h: exp(-2*pi*i*j/64), j in [0,64), as exact float hex literals.
 
-The register-level DFTs (radix <= 32) take their internal twiddles from this
-table at compile time.  Values are computed in double and rounded once to float.
+The register-level DFTs (radix <= 32) and the compile-time twiddle factors of the row
+passes (orders <= 64) take their twiddles from this table at compile time.  Values are
+computed in double and rounded once to float (entry 2j equals exp(-2*pi*i*j/32)
+exactly: the double arguments are the same).
 """
 import math
 import os
@@ -18,11 +20,11 @@ def f32hex(v):
 lines = ["// Generated by gen_twiddle32.py -- do not edit.",
          "#pragma once",
          "namespace cupssgb {",
-         "// kTw32Re[j] + i*kTw32Im[j] = exp(-2*pi*i*j/32)",
-         "constexpr float kTw32Re[32] = {"]
-lines.append(", ".join(f32hex(math.cos(2 * math.pi * j / 32)) for j in range(32)) + "};")
-lines.append("constexpr float kTw32Im[32] = {")
-lines.append(", ".join(f32hex(-math.sin(2 * math.pi * j / 32)) for j in range(32)) + "};")
+         "// kTw64Re[j] + i*kTw64Im[j] = exp(-2*pi*i*j/64)",
+         "constexpr float kTw64Re[64] = {"]
+lines.append(", ".join(f32hex(math.cos(2 * math.pi * j / 64)) for j in range(64)) + "};")
+lines.append("constexpr float kTw64Im[64] = {")
+lines.append(", ".join(f32hex(-math.sin(2 * math.pi * j / 64)) for j in range(64)) + "};")
 lines.append("}  // namespace cupssgb")
 here = os.path.dirname(os.path.abspath(__file__))
 with open(os.path.join(here, "twiddle32.h"), "w") as fh:

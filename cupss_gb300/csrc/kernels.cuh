@@ -77,15 +77,60 @@ __device__ __forceinline__ void static_for(iseq<I...>, F&& f) {
 // Twiddle W_sx^k of register I of thread m in the step-2 layout of a packed row
 // (k = m + M (j + J k'), I = j M + k'), from W_sx^m: W_sx^k = W_sx^m W_{2R}^{j + J k'}, the
 // second factor a compile-time constant (sx = 2 R M).  One table load per thread instead
-// of one per register; usable while 2R <= 32 (the compile-time twiddle table).
+// of one per register; usable while 2R <= 64 (the compile-time twiddle table).
 template <int LX>
 struct RowTwSplit {
-  static constexpr bool value = (2 * LineCfg<LX>::R <= 32) && (LineCfg<LX>::M > 1);
+  static constexpr bool value = (2 * LineCfg<LX>::R <= 64) && (LineCfg<LX>::M > 1);
 };
 template <int LX, int I>
 __device__ __forceinline__ float2 row_twiddle(float2 wm) {
   constexpr int M = LineCfg<LX>::M, R = LineCfg<LX>::R, J = R / M;
   return tw_const<2 * R, I / M + J * (I % M), false>(wm);
+}
+
+// C2R pre-processing of a packed row held in step-2 layout (v) and also stored in T
+// (padded positions): v[i] <- Z at k = pos_step2(m, i), the mirror X[Lx - k] from T.
+template <int LX>
+__device__ __forceinline__ void row_c2r(float2 (&v)[LineCfg<LX>::R], const float2* T, int m, const float2* tw) {
+  constexpr int R = LineCfg<LX>::R, sx = 2 * LX;
+  if constexpr (RowTwSplit<LX>::value) {
+    const float2 wm = tw_load(tw, sx, m);
+    static_for(make_iseq<R>{}, [&](auto I) {
+      constexpr int i = decltype(I)::value;
+      const int k = pos_step2<LX>(m, i);
+      v[i] = c2r_pre_w(v[i], T[pad_pos<LX>((LX - k) & (LX - 1))], k, row_twiddle<LX, i>(wm));
+    });
+  } else {
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int k = pos_step2<LX>(m, i);
+      v[i] = c2r_pre(v[i], T[pad_pos<LX>((LX - k) & (LX - 1))], k, sx, tw);
+    }
+  }
+}
+
+// R2C post-processing of a transformed row (v in step-2 layout, also stored in T) and
+// its store to out (packed row).
+template <int LX>
+__device__ __forceinline__ void row_r2c_store(const float2 (&v)[LineCfg<LX>::R], const float2* T, int m,
+                                              const float2* tw, float2* out, bool live) {
+  constexpr int R = LineCfg<LX>::R, sx = 2 * LX;
+  if constexpr (RowTwSplit<LX>::value) {
+    const float2 wm = tw_load(tw, sx, m);
+    static_for(make_iseq<R>{}, [&](auto I) {
+      constexpr int i = decltype(I)::value;
+      const int k = pos_step2<LX>(m, i);
+      const float2 x = r2c_post_w(v[i], T[pad_pos<LX>((LX - k) & (LX - 1))], k, row_twiddle<LX, i>(wm));
+      if (live) out[k] = x;
+    });
+  } else {
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int k = pos_step2<LX>(m, i);
+      const float2 x = r2c_post(v[i], T[pad_pos<LX>((LX - k) & (LX - 1))], k, sx, tw);
+      if (live) out[k] = x;
+    }
+  }
 }
 
 template <int LX>
@@ -153,11 +198,7 @@ row_pass(const XParams p) {
       T[pad_pos<LX>(k)] = v[i];
     }
     __syncthreads();
-#pragma unroll
-    for (int i = 0; i < R; ++i) {
-      const int k = pos_step2<LX>(m, i);
-      v[i] = c2r_pre(v[i], T[pad_pos<LX>((LX - k) & (LX - 1))], k, sx, p.tw);
-    }
+    row_c2r<LX>(v, T, m, p.tw);
     inv_step2<LX>(v);
     __syncthreads();
 #pragma unroll
@@ -210,14 +251,7 @@ row_pass(const XParams p) {
 #pragma unroll
     for (int i = 0; i < R; ++i) T[pad_pos<LX>(pos_step2<LX>(m, i))] = v[i];
     __syncthreads();
-    float2* out = reinterpret_cast<float2*>(p.out[q]) + rowoff;
-#pragma unroll
-    for (int i = 0; i < R; ++i) {
-      const int k = pos_step2<LX>(m, i);
-      const float2 zm = T[pad_pos<LX>((LX - k) & (LX - 1))];
-      const float2 x = r2c_post(v[i], zm, k, sx, p.tw);
-      if (live) out[k] = x;
-    }
+    row_r2c_store<LX>(v, T, m, p.tw, reinterpret_cast<float2*>(p.out[q]) + rowoff, live);
   }
 }
 
@@ -229,7 +263,7 @@ row_pass(const XParams p) {
 template <int LX>
 struct RowOneCfg {
   // resident CTAs per SM the register budget is sized for (RW*M = 128 threads each)
-  static constexpr int kMinBlocks = (LX <= 256) ? 4 : 2;
+  static constexpr int kMinBlocks = (LX <= 256) ? 4 : ((LX <= 512) ? 3 : 2);
 };
 
 template <int LX>
@@ -257,20 +291,7 @@ row_pass_one(const XParams p) {
     T[pad_pos<LX>(k)] = v[i];
   }
   __syncthreads();
-  if constexpr (RowTwSplit<LX>::value) {
-    const float2 wm = tw_load(p.tw, sx, m);
-    static_for(make_iseq<R>{}, [&](auto I) {
-      constexpr int i = decltype(I)::value;
-      const int k = pos_step2<LX>(m, i);
-      v[i] = c2r_pre_w(v[i], T[pad_pos<LX>((LX - k) & (LX - 1))], k, row_twiddle<LX, i>(wm));
-    });
-  } else {
-#pragma unroll
-    for (int i = 0; i < R; ++i) {
-      const int k = pos_step2<LX>(m, i);
-      v[i] = c2r_pre(v[i], T[pad_pos<LX>((LX - k) & (LX - 1))], k, sx, p.tw);
-    }
-  }
+  row_c2r<LX>(v, T, m, p.tw);
   inv_step2<LX>(v);
   __syncthreads();
 #pragma unroll
@@ -303,24 +324,7 @@ row_pass_one(const XParams p) {
 #pragma unroll
   for (int i = 0; i < R; ++i) T[pad_pos<LX>(pos_step2<LX>(m, i))] = v[i];
   __syncthreads();
-  float2* out = reinterpret_cast<float2*>(p.out[0]) + rowoff;
-  if constexpr (RowTwSplit<LX>::value) {
-    const float2 wm = tw_load(p.tw, sx, m);
-    static_for(make_iseq<R>{}, [&](auto I) {
-      constexpr int i = decltype(I)::value;
-      const int k = pos_step2<LX>(m, i);
-      const float2 x = r2c_post_w(v[i], T[pad_pos<LX>((LX - k) & (LX - 1))], k, row_twiddle<LX, i>(wm));
-      if (live) out[k] = x;
-    });
-  } else {
-#pragma unroll
-    for (int i = 0; i < R; ++i) {
-      const int k = pos_step2<LX>(m, i);
-      const float2 zm = T[pad_pos<LX>((LX - k) & (LX - 1))];
-      const float2 x = r2c_post(v[i], zm, k, sx, p.tw);
-      if (live) out[k] = x;
-    }
-  }
+  row_r2c_store<LX>(v, T, m, p.tw, reinterpret_cast<float2*>(p.out[0]) + rowoff, live);
 }
 
 // ------------------------------------------------------------------------------------

@@ -73,12 +73,14 @@ struct Fetch {
   int slot_sz, as, ap;
   int n_prod, wsel;
   float2 xi;
+  bool p0_reg;   // product 0 of this mode is p0 (kept in registers), not in its slot
+  float2 p0;
   __device__ __forceinline__ float2 get(int slot) const {
     const float2* S = smem + slot * slot_sz;
     if (wsel < 0) return S[as];
     return unpack(S[as], S[ap], wsel);
   }
-  __device__ __forceinline__ float2 prod(int c) const { return get(c); }
+  __device__ __forceinline__ float2 prod(int c) const { return (p0_reg && c == 0) ? p0 : get(c); }
   __device__ __forceinline__ float2 src(int j) const { return get(n_prod + j); }
 };
 
@@ -169,7 +171,8 @@ __device__ __forceinline__ void draw_line_noise(const LineParams& P, const Noise
 template <int L, bool Z3, class Prog, class G>
 __device__ __forceinline__ float2 update_mode(const LineParams& P, const LinePre& lp, const FieldK& F, int fi,
                                               const G& g, int i, const float2* smem, int n_prod, bool has_chan,
-                                              bool keep_fixed, float2 xi) {
+                                              bool keep_fixed, float2 xi, bool p0_reg = false,
+                                              float2 p0 = float2{0.f, 0.f}) {
   const int C = pos_step2<L>(0, i);
   const int pos = g.m + C;
   Fetch fx;
@@ -180,6 +183,8 @@ __device__ __forceinline__ float2 update_mode(const LineParams& P, const LinePre
   fx.n_prod = n_prod;
   fx.wsel = -1;
   fx.xi = xi;
+  fx.p0_reg = p0_reg;
+  fx.p0 = p0;
   const VPoint vp = line_vpoint<L, Z3>(P, lp, g.m, C);
   const float2 z = Prog::eval(P, fi, vp, fx);
   g.at(F.next)[g.elem(pos)] = z;
@@ -230,6 +235,10 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
     if (nf > 0 && plain && P.f[0].noisy)
       draw_line_noise<L>(P, nk, P.f[0].fid, line_pre<Z3>(P, d, g.kxp, g.lineky, m), xi0);
   }
+  // One field and one product (the Cahn-Hilliard form): the transformed product stays in
+  // v, at the modes the thread updates, unless a thread of the CTA reads a Hermitian
+  // partner's value (the packed column: its own tiles in 3D, tile 0 in 2D).  CTA-uniform.
+  const bool p0_reg = Prog::kUnroll && Spec::kNF == 1 && Spec::kNProd == 1 && (Z3 ? !g.packed_tile : g.kx0 > 0);
   for (int c = 0; c < n_prod; ++c) {
     float2* Sl = smem + c * slot_sz;
     if (c > 0) load_product(c);
@@ -240,6 +249,7 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
 #pragma unroll
     for (int i = 0; i < R; ++i) v[i] = Sl[g.sidx(l, pos_t2<L>(m, i))];
     fwd_step2<L>(v);
+    if (p0_reg) break;   // the only product: kept in v
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < R; ++i) Sl[g.sidx(l, pos_step2<L>(m, i))] = v[i];
@@ -249,7 +259,10 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
     const FieldK& F = P.f[fi];
     const bool has_chan = (F.chan != nullptr);
     cp_async_wait_all();
-    __syncthreads();   // this field's states and every product slot are in place
+    // this field's states and every product slot are in place for the whole CTA (with the
+    // product in registers every thread reads only its own copies: its wait suffices; the
+    // barrier before the inverse transform keeps slot 0's transposes apart)
+    if (!p0_reg) __syncthreads();
     // 2) pointwise update.  Columns kx' > 0: plain half-spectrum modes; with a
     // generated program (Prog::kUnroll) the R points are unrolled so that their
     // independent arithmetic overlaps, the noise draws first (independent generator
@@ -273,7 +286,8 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
         }
 #pragma unroll
         for (int i = 0; i < R; ++i)
-          ch[i] = update_mode<L, Z3, Prog>(P, lp, F, fi, g, i, smem, n_prod, has_chan, keep_fixed, ch[i]);
+          ch[i] = update_mode<L, Z3, Prog>(P, lp, F, fi, g, i, smem, n_prod, has_chan, keep_fixed, ch[i], p0_reg,
+                                           v[i]);
       } else {
         // table-driven program: a rolled loop (its unrolled code would be very large);
         // the results go through a thread-local array into the registers
@@ -307,6 +321,7 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
         fx.as = g.sidx(l, pos);
         fx.ap = g.sidx(pl, ppos);
         fx.n_prod = n_prod;
+        fx.p0_reg = false;
         fx.wsel = 0;
         const VPoint v0 = make_vpoint(P, d, 0, ky, kz);
         fx.xi = F.noisy ? noise_at(P, d, nk, F.fid, 0, ky, kz) : make_float2(0.f, 0.f);

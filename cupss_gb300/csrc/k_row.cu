@@ -17,7 +17,7 @@ static cudaError_t launch_row_t(const XParams& p, cudaStream_t st, int nz, bool 
   dim3 block(C::M, C::RW);
   dim3 grid((p.rows + C::RW - 1) / C::RW, 1, nz);
   if (row_is_one(p)) {
-    const size_t smem = (size_t)C::RW * C::PL * sizeof(float2);
+    const size_t smem = 2 * (size_t)C::RW * C::PL * sizeof(float2);   // two transpose buffers
     if (!attr_one) {
       cudaError_t e = cudaFuncSetAttribute(row_pass_one<LX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            220 * 1024);

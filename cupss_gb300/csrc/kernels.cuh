@@ -257,9 +257,9 @@ row_pass(const XParams p) {
 
 // Single spectral input, single spectral product (the Cahn-Hilliard form phi^n): the
 // inverse transform of the row stays in registers and feeds the product and the forward
-// transform directly, so shared memory holds only the transpose buffer (one slot instead
-// of two) and the input is read once instead of once per factor.  Columns at or beyond
-// in_xcols[0] are known zero (dealiased channel) and are not loaded.
+// transform directly, so shared memory holds only transpose buffers (no slot for the
+// real-space input) and the input is read once instead of once per factor.  Columns at
+// or beyond in_xcols[0] are known zero (dealiased channel) and are not loaded.
 template <int LX>
 struct RowOneCfg {
   // resident CTAs per SM the register budget is sized for (RW*M = 128 threads each)
@@ -278,8 +278,11 @@ row_pass_one(const XParams p) {
   const int rl = threadIdx.y;
   const int row = blockIdx.x * RW + rl;
   const bool live = row < p.rows;
-  const int sx = 2 * LX;
-  float2* T = smem + rl * PL;
+  // two transpose buffers used in turn: a buffer is written again only after a barrier
+  // that follows every read of its previous contents, so the write-after-read barriers
+  // of a single buffer are not needed
+  float2* TA = smem + rl * PL;
+  float2* TB = smem + (RW + rl) * PL;
   const size_t rowoff = (size_t)blockIdx.z * p.mstride + (size_t)(live ? row : 0) * LX;
   const int xcols = p.in_xcols[0] > 0 ? p.in_xcols[0] : LX;
   float2 v[R];
@@ -288,17 +291,16 @@ row_pass_one(const XParams p) {
   for (int i = 0; i < R; ++i) {
     const int k = pos_step2<LX>(m, i);
     v[i] = (live && k < xcols) ? in[k] : make_float2(0.f, 0.f);
-    T[pad_pos<LX>(k)] = v[i];
+    TA[pad_pos<LX>(k)] = v[i];
   }
   __syncthreads();
-  row_c2r<LX>(v, T, m, p.tw);
+  row_c2r<LX>(v, TA, m, p.tw);
   inv_step2<LX>(v);
+#pragma unroll
+  for (int i = 0; i < R; ++i) TB[pad_pos<LX>(pos_t2<LX>(m, i))] = v[i];
   __syncthreads();
 #pragma unroll
-  for (int i = 0; i < R; ++i) T[pad_pos<LX>(pos_t2<LX>(m, i))] = v[i];
-  __syncthreads();
-#pragma unroll
-  for (int s = 0; s < R; ++s) v[s] = T[pad_pos<LX>(pos_t1<LX>(m, s))];
+  for (int s = 0; s < R; ++s) v[s] = TB[pad_pos<LX>(pos_t1<LX>(m, s))];
   inv_step1<LX>(v, m, p.tw);
   // v[r] = real pair (r[2n], r[2n+1]) at n = m + M r: raise to the product's order
   const int order = p.prod_n[0];
@@ -313,18 +315,16 @@ row_pass_one(const XParams p) {
     v[r] = acc;
   }
   fwd_step1<LX>(v, m, p.tw);
+#pragma unroll
+  for (int s = 0; s < R; ++s) TA[pad_pos<LX>(pos_t1<LX>(m, s))] = v[s];
   __syncthreads();
 #pragma unroll
-  for (int s = 0; s < R; ++s) T[pad_pos<LX>(pos_t1<LX>(m, s))] = v[s];
-  __syncthreads();
-#pragma unroll
-  for (int i = 0; i < R; ++i) v[i] = T[pad_pos<LX>(pos_t2<LX>(m, i))];
+  for (int i = 0; i < R; ++i) v[i] = TA[pad_pos<LX>(pos_t2<LX>(m, i))];
   fwd_step2<LX>(v);
-  __syncthreads();
 #pragma unroll
-  for (int i = 0; i < R; ++i) T[pad_pos<LX>(pos_step2<LX>(m, i))] = v[i];
+  for (int i = 0; i < R; ++i) TB[pad_pos<LX>(pos_step2<LX>(m, i))] = v[i];
   __syncthreads();
-  row_r2c_store<LX>(v, T, m, p.tw, reinterpret_cast<float2*>(p.out[0]) + rowoff, live);
+  row_r2c_store<LX>(v, TB, m, p.tw, reinterpret_cast<float2*>(p.out[0]) + rowoff, live);
 }
 
 // ------------------------------------------------------------------------------------
@@ -351,7 +351,7 @@ line_pass(const LineParams P) {
 #pragma unroll
       for (int r = 0; r < R; ++r) v[r] = g.ok ? in[g.elem(pos_step1<L>(g.m, r))] : make_float2(0.f, 0.f);
       fwd_step1<L>(v, g.m, P.tw);
-      __syncthreads();
+      if (c > 0) __syncthreads();   // the previous channel's reads of T
 #pragma unroll
       for (int s = 0; s < R; ++s) T[g.sidx(0, pos_t1<L>(g.m, s))] = v[s];
       __syncthreads();
@@ -371,7 +371,7 @@ line_pass(const LineParams P) {
         v[i] = (g.ok && (keep <= 0 || nk < keep)) ? in[g.elem(k)] : make_float2(0.f, 0.f);
       }
       inv_step2<L>(v);
-      __syncthreads();
+      if (c > 0) __syncthreads();   // the previous channel's reads of T
 #pragma unroll
       for (int i = 0; i < R; ++i) T[g.sidx(0, pos_t2<L>(g.m, i))] = v[i];
       __syncthreads();

@@ -34,6 +34,33 @@ __device__ __forceinline__ void philox4x32_10(uint32_t& c0, uint32_t& c1, uint32
   }
 }
 
+// NB independent Philox4x32-10 blocks c[b] under one key, advanced round by round: the
+// rounds form a loop (not unrolled) whose body updates all NB blocks, so the blocks'
+// independent multiply chains overlap while the code stays NB rounds long.  Same values
+// as philox4x32_10 on each block.
+template <int NB>
+__device__ __forceinline__ void philox4x32_10_batch(uint32_t (&c)[NB][4], uint32_t k0, uint32_t k1) {
+  constexpr uint32_t kM0 = 0xD2511F53u, kM1 = 0xCD9E8D57u;
+  constexpr uint32_t kW0 = 0x9E3779B9u, kW1 = 0xBB67AE85u;
+#pragma unroll 1
+  for (int r = 0; r < 10; ++r) {
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const unsigned long long p0 = (unsigned long long)kM0 * c[b][0];
+      const unsigned long long p1 = (unsigned long long)kM1 * c[b][2];
+      const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+      const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+      const uint32_t n0 = hi1 ^ c[b][1] ^ k0, n2 = hi0 ^ c[b][3] ^ k1;
+      c[b][0] = n0;
+      c[b][1] = lo1;
+      c[b][2] = n2;
+      c[b][3] = lo0;
+    }
+    k0 += kW0;
+    k1 += kW1;
+  }
+}
+
 // Box-Muller: two standard normals from two 32-bit words.
 //   u1 = ((a >> 8) + 1) 2^-24 in (0, 1],  u2 = (b >> 8) 2^-24 in [0, 1)
 //   r = sqrt(-2 ln u1),  theta = 2 pi (u2 - 1/2) in [-pi, pi)

@@ -148,22 +148,37 @@ struct RtSpec {
 // or when the field has no dealiased copy).
 // Fourier noise of a thread's R plain modes of one line, drawn in (t, t + Lt/2) pairs
 // (one generator call per pair).
+// The lower registers (positions t < L/2) in order: register of pair p.
+template <int L>
+__host__ __device__ constexpr int lower_reg(int p) {
+  constexpr int Mx = LineCfg<L>::M;
+  return (L == 1) ? 0 : ((Mx >= 2) ? (p / (Mx / 2)) * Mx + p % (Mx / 2) : p);
+}
+
 template <int L>
 __device__ __forceinline__ void draw_line_noise(const LineParams& P, const NoiseKey& nk, int fid, const LinePre& lp,
                                                 float2 (&xi)[LineCfg<L>::R]) {
   constexpr int R = LineCfg<L>::R;
   constexpr int Mx = LineCfg<L>::M;
   constexpr int HALF = (Mx >= 2) ? Mx / 2 : R / 2;   // register offset of t + L/2
+  constexpr int NP = (L == 1) ? 1 : R / 2;            // generator calls: one per pair
+  uint32_t c[NP][4];
 #pragma unroll
-  for (int i = 0; i < R; ++i) {
-    const int kp = (Mx >= 2) ? (i % Mx) : (i / Mx);
-    const bool lower = (L == 1) || ((Mx >= 2) ? (kp < Mx / 2) : (kp < R / 2));
-    if (lower) {
-      float2 lo, hi;
-      noise_pair_lin(P, nk, fid, lp.lin0 + (uint32_t)pos_step2<L>(0, i) * lp.lin_step, lo, hi);
-      xi[i] = lo;
-      if (L > 1) xi[i + HALF] = hi;
-    }
+  for (int q = 0; q < NP; ++q) {
+    c[q][0] = lp.lin0 + (uint32_t)pos_step2<L>(0, lower_reg<L>(q)) * lp.lin_step;
+    c[q][1] = nk.step;
+    c[q][2] = (uint32_t)fid;
+    c[q][3] = 0u;
+  }
+  philox4x32_10_batch<NP>(c, nk.key0, nk.key1);
+#pragma unroll
+  for (int q = 0; q < NP; ++q) {
+    const int i = lower_reg<L>(q);
+    float g1, g2, g3, g4;
+    box_muller(c[q][0], c[q][1], g1, g2);
+    box_muller(c[q][2], c[q][3], g3, g4);
+    xi[i] = make_float2(P.sqrtHalfN * g1, P.sqrtHalfN * g2);
+    if (L > 1) xi[i + HALF] = make_float2(P.sqrtHalfN * g3, P.sqrtHalfN * g4);
   }
 }
 

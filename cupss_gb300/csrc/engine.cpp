@@ -264,21 +264,47 @@ void Solver::prepare() {
       int nslots = 0;
       bool any_chan = false;
       fill_turn(P, p, nslots, any_chan);
-      p.W = P.tuned_w > 0 ? P.tuned_w : pick_w(L, nl, nslots);
+      p.W = P.tuned_w > 0 ? P.tuned_w : pick_w(L, nl, nslots, turn_rows(), turn_split());
+      if (turn_w_ > 0 && turn_w_ < p.W && P.tuned_w <= 0) p.W = turn_w_;
       jit_kernel(turn_source(P, p, L, nl), "cupssgb_turn");
     }
   }
 }
 
-int Solver::pick_w(int L, int nl, int nslots) const {
+// Multiprocessors of the current device (152 on a GB300; also the answer without a GPU).
+static int sm_count() {
+  static int n = 0;
+  if (n > 0) return n;
+  int dev = 0, v = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) !=
+                                                cudaSuccess || v <= 0) {
+    cudaGetLastError();
+    return 152;
+  }
+  n = v;
+  return n;
+}
+
+bool Solver::turn_split() const {
+  return use_jit_ && turn_split_form(dim_ == 3 ? sz_ : sy_, dim_ == 3 ? 2 : 1);
+}
+
+int Solver::pick_w(int L, int nl, int nslots, int other, bool split) const {
   int W = 16;
   while (W > Lx_) W /= 2;
   if (W < 1) W = 1;
-  while (W > 1 && (line_threads(L, nl, W) > 256 ||
-                   line_pass_smem(L, nl, W, std::max(nslots, 1)) > 200 * 1024))
+  while (W > 1 && (line_threads(L, nl, W, split) > 256 ||
+                   line_pass_smem(L, nl, W, std::max(nslots, 1), split) > 200 * 1024))
     W /= 2;
-  if (line_pass_smem(L, nl, W, std::max(nslots, 1)) > 220 * 1024)
+  if (line_pass_smem(L, nl, W, std::max(nslots, 1), split) > 220 * 1024)
     throw Error(kErrLimit, "phase needs more shared memory than one CTA has");
+  // a single system whose grid has fewer tiles than the GPU has SMs (2D grids with long
+  // lines): narrower tiles put every SM to work.  Batches multiply the tiles by their
+  // members and tune the width by measurement instead.
+  if (!batch_ && other > 0) {
+    const int sms = sm_count();
+    while (W > 2 && (long long)((Lx_ + W - 1) / W) * other < sms) W /= 2;
+  }
   return W;
 }
 
@@ -307,7 +333,7 @@ void Solver::line_fwd_inv(int geo, int mode, const float2* in, float2* out, int 
   LineParams p;
   const int L = (geo == kGeoY3 || geo == kGeoCol) ? sy_ : sz_;
   fill_line_common(p, L, geo, mode);
-  p.W = pick_w(L, 1, 1);
+  p.W = pick_w(L, 1, 1, geo == kGeoY3 ? sz_ : (geo == kGeoZ3 ? sy_ : 1));
   p.n_prod = 1;
   p.prod_in[0] = in;
   p.prod_out[0] = out;
@@ -756,7 +782,7 @@ void Solver::run_phase(Phase& P) {
   int nslots = 0;
   bool any_chan = false;
   fill_turn(P, p, nslots, any_chan);
-  p.W = pick_w(L, nl, nslots);
+  p.W = pick_w(L, nl, nslots, turn_rows(), turn_split());
   if (turn_w_ > 0 && turn_w_ < p.W) p.W = turn_w_;
   if (P.tuned_w > 0) p.W = P.tuned_w;
   p.members = members_d_;
@@ -776,9 +802,9 @@ void Solver::run_phase(Phase& P) {
     if (tuning_) ps.W = 0;
     const std::string& src = turn_source(P, ps, L, nl);
     cudaKernel_t k = jit_kernel(src, "cupssgb_turn");
-    dim3 block(p.W, line_threads(L, 1, 1), nl);
+    dim3 block(p.W, line_threads(L, 1, 1, turn_split()), nl);
     void* args[] = {(void*)&p};
-    LaunchCfg lc(grid, block, line_pass_smem(L, nl, p.W, nslots), stream_, pdl_);
+    LaunchCfg lc(grid, block, line_pass_smem(L, nl, p.W, nslots, turn_split()), stream_, pdl_);
     check(cudaLaunchKernelExC(&lc.cfg, (const void*)k, args), "turnaround (generated)");
   } else {
     check(launch_line_pass(p, nl, nslots, grid, stream_, pdl_), "turnaround");

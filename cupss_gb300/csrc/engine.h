@@ -10,6 +10,7 @@
 // doing the Fourier-space update], with 3D adding a y-axis pass on either side.
 #pragma once
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -151,7 +152,12 @@ class Solver {
                  const std::vector<HostField>* fields = nullptr) const;
   const std::string& turn_source(Phase& P, const LineParams& p, int L, int nl);
   void fill_line_common(LineParams& p, int L, int geo, int mode) const;
-  int pick_w(int L, int nl, int nslots) const;
+  // other: CTAs of the launch along its second grid axis (0: no SM-coverage rule);
+  // split: the lines use the split FFT form
+  int pick_w(int L, int nl, int nslots, int other = 0, bool split = false) const;
+  int turn_rows() const { return dim_ == 3 ? std::max(sy_ / 2, 1) : 1; }
+  // the turnaround runs the generated kernel with lines in the split FFT form
+  bool turn_split() const;
   // lkeep > 0: inverse-pass input positions with |n| >= lkeep along the line are zero
   void line_fwd_inv(int geo, int mode, const float2* in, float2* out, int xlimit, bool batch = false,
                     int lkeep = 0, bool pdl = false);

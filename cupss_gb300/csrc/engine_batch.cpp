@@ -214,7 +214,7 @@ void Solver::autotune() {
     int nslots = 0;
     bool any_chan = false;
     fill_turn(P, p, nslots, any_chan);
-    const int wmax = pick_w(L, nl, nslots);
+    const int wmax = pick_w(L, nl, nslots, 0, turn_split());
     if (turn_w_ > 0) {
       P.tuned_w = std::min(turn_w_, wmax);
       continue;

@@ -1,22 +1,34 @@
 // Register/shared-memory FFT building blocks for the GB300 pseudospectral engine.
 //
-// A line of length L (power of two, 1..1024) is split as L = R * M with
-// M = 2^floor(log2(L)/2) and R = L / M (so R is M or 2M).  M threads cooperate on
-// one line; each thread holds R complex values in registers.
+// A line of length L (power of two, 1..1024) is split as L = R * M: M threads cooperate
+// on one line and each holds R complex values in registers.  The four-step form uses
+// M = 2^floor(log2(L)/2) (R is M or 2M).  Lines of 512 and 1024 points can instead take
+// the split form below (template flag SP): R = 16 and M = L/16 threads, so that a pass
+// over few long lines (a 2D grid) still gives the GPU enough threads.
 //
 //   step-1 layout: thread m holds positions  n = m + M*r,            r in [0,R)
 //   step-2 layout: thread m holds positions  k = s + R*k',  s = m + M*j,
 //                  j in [0, R/M), k' in [0,M)   (register index j*M + k')
+//                  split form: k = m + M*f      (register index f)
 //
 // Forward transform (unnormalised, exp(-2 pi i n k / L)):
 //   fwd_step1 (radix-R DFT over r, twiddle W_L^{m s}), store to the transpose
-//   buffer at position s*M + m, sync, load positions s*M + k, fwd_step2 (radix-M).
+//   buffer at position s*M + m, sync, fwd_load_step2 (load, radix-M).
 // Inverse transform (unnormalised, exp(+2 pi i n k / L)) runs the same steps
-// backwards: inv_step2 in step-2 layout, transpose, inv_step1.
+// backwards: inv_step2 in step-2 layout, inv_store_t, sync, inv_load_step1.
 //
 // The four-step split X[s + R k'] = sum_m W_M^{m k'} W_L^{m s} sum_r x[m + M r] W_R^{r s}
 // is the standard Cooley-Tukey factorisation; the register DFTs are recursive
 // radix-2 decimation in time with compile-time twiddles.
+//
+// Split form (M = G*R threads, G = 2 or 4): the radix-M DFT of step 2 is itself split
+// with m = a + R b, k' = e + G f (a, f in [0,R); b, e in [0,G)):
+//   X[s + R (e + G f)] = sum_a W_R^{a f} W_M^{a e} sum_b W_G^{b e} Y_{a + R b}[s],
+// Y_m[s] the step-1 output of thread m.  Thread m' = s + R e loads the G values of each
+// a from row s of the transpose buffer and sums them with the roots W_G^{b e} (+-1, +-i,
+// exact), twiddles and runs a radix-R DFT over a; its outputs k = m' + M f are cyclic like
+// the step-1 inputs.  The inverse runs the same steps backwards: radix-R over f, twiddle,
+// store at s*M + e*R + a, sync, thread m = a + R b sums the G values of each s.
 #pragma once
 #if !defined(__CUDACC_RTC__)
 #include <cuda_runtime.h>
@@ -153,16 +165,26 @@ struct Dft {
   }
 };
 
-template <int L>
+template <int L, bool SP = false>
 struct LineCfg {
   static constexpr int lg = (L <= 1) ? 0 : (L == 2 ? 1 : (L == 4 ? 2 : (L == 8 ? 3 : (L == 16 ? 4 :
                             (L == 32 ? 5 : (L == 64 ? 6 : (L == 128 ? 7 : (L == 256 ? 8 :
                             (L == 512 ? 9 : (L == 1024 ? 10 : -1))))))))));
   static_assert(lg >= 0, "line length must be a power of two in [1, 1024]");
-  static constexpr int M = 1 << (lg / 2);
-  static constexpr int R = L / M;
-  static constexpr int J = R / M;   // s-values per thread in step 2 (1 or 2)
+  static constexpr bool kSplit = SP && (L >= 512);
+  static constexpr int M = kSplit ? L / 16 : (1 << (lg / 2));   // threads per line
+  static constexpr int R = L / M;                               // values per thread
+  static constexpr int J = kSplit ? 1 : R / M;   // s-values per thread in step 2 (1 or 2)
+  static constexpr int G = kSplit ? M / R : 1;   // split form: threads per s-value in step 2
 };
+
+// Host-side threads per line (equals LineCfg<L, split>::M for every supported L).
+CG_HD int line_m_of(int L, bool split) {
+  if (split && L >= 512) return L / 16;
+  int lg = 0;
+  while ((1 << lg) < L) ++lg;
+  return 1 << (lg / 2);
+}
 
 // Twiddle super-table: the table for length L lives at tw + L and holds
 // exp(-2 pi i j / L) for j in [0, L).
@@ -180,76 +202,168 @@ CG_HD float2 tw_load(const float2* tw, int L, int j) {
 #endif
 }
 
-template <int L, bool INV>
-CG_HD void step_r(float2 (&v)[LineCfg<L>::R]) {
-  Dft<LineCfg<L>::R, INV, 1>::template run<0>(v);
+template <int L, bool INV, bool SP = false>
+CG_HD void step_r(float2 (&v)[LineCfg<L, SP>::R]) {
+  Dft<LineCfg<L, SP>::R, INV, 1>::template run<0>(v);
 }
 
 // Forward step 1: v[r] = x[m + M r] in, v[s] = W_L^{m s} * DFT_R(x[m + M .])[s] out.
-template <int L>
-CG_HD void fwd_step1(float2 (&v)[LineCfg<L>::R], int m, const float2* tw) {
-  constexpr int R = LineCfg<L>::R;
+template <int L, bool SP = false>
+CG_HD void fwd_step1(float2 (&v)[LineCfg<L, SP>::R], int m, const float2* tw) {
+  constexpr int R = LineCfg<L, SP>::R;
   Dft<R, false, 1>::template run<0>(v);
 #pragma unroll
   for (int s = 1; s < R; ++s) v[s] = c_mul(v[s], tw_load(tw, L, m * s));
 }
 
-// Forward step 2: register index j*M + k holds position s*M + k (s = m + M j) of the
-// transposed data; output register j*M + k' holds X[s + R k'].
-template <int L>
-CG_HD void fwd_step2(float2 (&v)[LineCfg<L>::R]) {
-  constexpr int M = LineCfg<L>::M;
-  constexpr int J = LineCfg<L>::J;
+// Step-2 DFTs of the four-step form: register index j*M + k holds position s*M + k
+// (s = m + M j) of the transposed data; output register j*M + k' holds X[s + R k'].
+template <int L, bool SP = false>
+CG_HD void fwd_dft2(float2 (&v)[LineCfg<L, SP>::R]) {
+  constexpr int M = LineCfg<L, SP>::M;
+  constexpr int J = LineCfg<L, SP>::J;
   if constexpr (J >= 1) Dft<M, false, 1>::template run<0>(v);
   if constexpr (J >= 2) Dft<M, false, 1>::template run<M>(v);
 }
-
-// Inverse step 2: register j*M + k' holds X[s + R k']; out register j*M + m' holds
+// register j*M + k' holds X[s + R k']; out register j*M + m' holds
 // y_{m'}[s] = sum_k' X[s + R k'] W_M^{-m' k'}  (to be stored at position s*M + m').
-template <int L>
-CG_HD void inv_step2(float2 (&v)[LineCfg<L>::R]) {
-  constexpr int M = LineCfg<L>::M;
-  constexpr int J = LineCfg<L>::J;
+template <int L, bool SP = false>
+CG_HD void inv_dft2(float2 (&v)[LineCfg<L, SP>::R]) {
+  constexpr int M = LineCfg<L, SP>::M;
+  constexpr int J = LineCfg<L, SP>::J;
   if constexpr (J >= 1) Dft<M, true, 1>::template run<0>(v);
   if constexpr (J >= 2) Dft<M, true, 1>::template run<M>(v);
 }
 
+// W_G^q = exp(-2 pi i q / G) for G = 2 or 4: one of +-1, +-i, exact.
+template <int G>
+CG_HD float2 root_g(int q) {
+  const int qq = (q * (4 / G)) & 3;
+  return make_float2(qq == 0 ? 1.f : (qq == 2 ? -1.f : 0.f), qq == 1 ? -1.f : (qq == 3 ? 1.f : 0.f));
+}
+
 // Inverse step 1: v[s] = y_m[s] (loaded from positions s*M + m) in,
 // v[r] = x[m + M r] out.
-template <int L>
-CG_HD void inv_step1(float2 (&v)[LineCfg<L>::R], int m, const float2* tw) {
-  constexpr int R = LineCfg<L>::R;
+template <int L, bool SP = false>
+CG_HD void inv_step1(float2 (&v)[LineCfg<L, SP>::R], int m, const float2* tw) {
+  constexpr int R = LineCfg<L, SP>::R;
 #pragma unroll
   for (int s = 1; s < R; ++s) v[s] = c_mulc(v[s], tw_load(tw, L, m * s));
   Dft<R, true, 1>::template run<0>(v);
 }
 
-// Position of register index idx in the step-1 / step-2 layouts.
-template <int L>
-CG_HD int pos_step1(int m, int r) { return m + LineCfg<L>::M * r; }
-template <int L>
-CG_HD int pos_step2(int m, int idx) {
-  constexpr int M = LineCfg<L>::M;
-  constexpr int R = LineCfg<L>::R;
-  const int j = idx / M, kp = idx % M;
-  return (m + M * j) + R * kp;
-}
-// Transpose-buffer position written after fwd_step1 for value s, and read before
-// fwd_step2 for register index idx (= j*M + k).
-template <int L>
-CG_HD int pos_t1(int m, int s) { return s * LineCfg<L>::M + m; }
-template <int L>
+// Transpose-buffer position written after fwd_step1 for value s.
+template <int L, bool SP = false>
+CG_HD int pos_t1(int m, int s) { return s * LineCfg<L, SP>::M + m; }
+// Four-step form: position read before step 2 for register index idx (= j*M + k).
+template <int L, bool SP = false>
 CG_HD int pos_t2(int m, int idx) {
-  constexpr int M = LineCfg<L>::M;
+  constexpr int M = LineCfg<L, SP>::M;
   const int j = idx / M, k = idx % M;
   return (m + M * j) * M + k;
 }
 
+// Forward step 2 after the transpose (the buffer holds every thread's fwd_step1 output
+// at pos_t1; ld(pos) reads the buffer at position pos): v[i] = X[pos_step2(m, i)] out.
+template <int L, bool SP = false, class Ld>
+CG_HD void fwd_load_step2(float2 (&v)[LineCfg<L, SP>::R], int m, const float2* tw, Ld&& ld) {
+  using C = LineCfg<L, SP>;
+  constexpr int M = C::M, R = C::R;
+  if constexpr (!C::kSplit) {
+#pragma unroll
+    for (int i = 0; i < R; ++i) v[i] = ld(pos_t2<L, SP>(m, i));
+    fwd_dft2<L, SP>(v);
+  } else {
+    constexpr int G = C::G;
+    const int s = m % R, e = m / R;
+    float2 w[G];
+#pragma unroll
+    for (int b = 0; b < G; ++b) w[b] = root_g<G>(b * e);
+#pragma unroll
+    for (int a = 0; a < R; ++a) {
+      float2 acc = ld(s * M + a);
+#pragma unroll
+      for (int b = 1; b < G; ++b) acc = c_add(acc, c_mul(ld(s * M + a + R * b), w[b]));
+      v[a] = acc;
+    }
+#pragma unroll
+    for (int a = 1; a < R; ++a) v[a] = c_mul(v[a], tw_load(tw, M, a * e));
+    Dft<R, false, 1>::template run<0>(v);
+  }
+}
+
+// Inverse step 2 in registers: v[i] = X[pos_step2(m, i)] in; out the values that
+// inv_store_t writes to the transpose buffer.
+template <int L, bool SP = false>
+CG_HD void inv_step2(float2 (&v)[LineCfg<L, SP>::R], int m, const float2* tw) {
+  using C = LineCfg<L, SP>;
+  constexpr int M = C::M, R = C::R;
+  if constexpr (!C::kSplit) {
+    inv_dft2<L, SP>(v);
+  } else {
+    Dft<R, true, 1>::template run<0>(v);
+    const int e = m / R;
+#pragma unroll
+    for (int a = 1; a < R; ++a) v[a] = c_mulc(v[a], tw_load(tw, M, a * e));
+  }
+}
+// Store of the inv_step2 output: st(pos, value) writes the transpose buffer.
+template <int L, bool SP = false, class St>
+CG_HD void inv_store_t(const float2 (&v)[LineCfg<L, SP>::R], int m, St&& st) {
+  using C = LineCfg<L, SP>;
+  constexpr int M = C::M, R = C::R;
+  if constexpr (!C::kSplit) {
+#pragma unroll
+    for (int i = 0; i < R; ++i) st(pos_t2<L, SP>(m, i), v[i]);
+  } else {
+    const int s = m % R, e = m / R;
+#pragma unroll
+    for (int a = 0; a < R; ++a) st(s * M + e * R + a, v[a]);
+  }
+}
+// After the transpose: loads and inverse step 1; v[r] = x[m + M r] out.
+template <int L, bool SP = false, class Ld>
+CG_HD void inv_load_step1(float2 (&v)[LineCfg<L, SP>::R], int m, const float2* tw, Ld&& ld) {
+  using C = LineCfg<L, SP>;
+  constexpr int M = C::M, R = C::R;
+  if constexpr (!C::kSplit) {
+#pragma unroll
+    for (int s = 0; s < R; ++s) v[s] = ld(pos_t1<L, SP>(m, s));
+  } else {
+    constexpr int G = C::G;
+    const int a = m % R, b = m / R;
+    float2 w[G];
+#pragma unroll
+    for (int e = 0; e < G; ++e) w[e] = root_g<G>(b * e);
+#pragma unroll
+    for (int s = 0; s < R; ++s) {
+      float2 acc = ld(s * M + a);
+#pragma unroll
+      for (int e = 1; e < G; ++e) acc = c_add(acc, c_mulc(ld(s * M + e * R + a), w[e]));
+      v[s] = acc;
+    }
+  }
+  inv_step1<L, SP>(v, m, tw);
+}
+
+// Position of register index idx in the step-1 / step-2 layouts.  Both are cyclic:
+// pos = m + step2_off(idx) with the offset a multiple of M.
+template <int L, bool SP = false>
+CG_HD int pos_step1(int m, int r) { return m + LineCfg<L, SP>::M * r; }
+template <int L, bool SP = false>
+CG_HD constexpr int step2_off(int idx) {
+  constexpr int M = LineCfg<L, SP>::M;
+  constexpr int R = LineCfg<L, SP>::R;
+  return LineCfg<L, SP>::kSplit ? M * idx : M * (idx / M) + R * (idx % M);
+}
+template <int L, bool SP = false>
+CG_HD int pos_step2(int m, int idx) { return m + step2_off<L, SP>(idx); }
+
 // Padded shared-memory index of position n: one pad slot every M positions keeps
 // the strided step-2 accesses free of bank conflicts.
-template <int L>
-CG_HD int pad_pos(int n) { return n + n / LineCfg<L>::M; }
-template <int L>
-CG_HD constexpr int padded_len() { return L + L / LineCfg<L>::M; }
+template <int L, bool SP = false>
+CG_HD int pad_pos(int n) { return n + n / LineCfg<L, SP>::M; }
+template <int L, bool SP = false>
+CG_HD constexpr int padded_len() { return L + L / LineCfg<L, SP>::M; }
 
 }  // namespace cupssgb

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "launch.h"
 #include "jit_headers.inc"
 
 namespace cupssgb {
@@ -70,8 +71,8 @@ std::string jit_generate_turn(const LineParams& p, int L, int NL, int warps, boo
                    : "P.f[" + std::to_string(fi) + "].noise_base";
   };
   // block = (W, M, NL) threads
-  int M = 1;
-  while (4 * M * M <= L) M *= 2;   // LineCfg<L>::M = 2^floor(log2(L)/2)
+  const bool split = turn_split_form(L, NL);
+  const int M = line_threads(L, 1, 1, split);   // LineCfg<L, split>::M
   const int threads = p.W > 0 ? p.W * M * NL : 256;
   const int min_blocks = std::max(1, warps * 32 / threads);
   // overlap of the first field's noise with the first product's loads: for spectra that
@@ -166,6 +167,7 @@ std::string jit_generate_turn(const LineParams& p, int L, int NL, int warps, boo
     << "  static constexpr int kSX = " << p.sx << ", kSY = " << p.sy << ", kSZ = " << p.sz << ";\n"
     << "  static constexpr int kW = " << p.W << ";\n"
     << "  static constexpr bool kEarlyNoise = " << (early_noise ? "true" : "false") << ";\n"
+    << "  static constexpr bool kSplit = " << (split ? "true" : "false") << ";\n"
     << "};\n}  // namespace cupssgb\n"
     << "extern \"C\" __global__ void __launch_bounds__(" << threads << ", " << min_blocks
     << ") cupssgb_turn(const cupssgb::LineParams P) {\n"

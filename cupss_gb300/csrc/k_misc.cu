@@ -1,20 +1,33 @@
 // Line-pass dispatch and the spectrum expansion kernel.
+#include <cstdlib>
 #include "kernels.cuh"
 #include "launch.h"
 
 namespace cupssgb {
 
-static int m_of(int L) {
-  int lg = 0;
-  while ((1 << lg) < L) ++lg;
-  return 1 << (lg / 2);
-}
-static int pl_of(int L) { return L + L / m_of(L); }
+static_assert(LineCfg<1>::M == 1 && LineCfg<8>::M == 2 && LineCfg<16>::M == 4 && LineCfg<256>::M == 16 &&
+                  LineCfg<512>::M == 16 && LineCfg<1024>::M == 32 && LineCfg<256, true>::M == 16 &&
+                  LineCfg<512, true>::M == 32 && LineCfg<1024, true>::M == 64,
+              "line_m_of must follow LineCfg");
+static int pl_of(int L, bool split) { return L + L / line_m_of(L, split); }
 
-size_t line_pass_smem(int L, int nl, int W, int nslots) {
-  return (size_t)nslots * nl * pl_of(L) * W * sizeof(float2);
+size_t line_pass_smem(int L, int nl, int W, int nslots, bool split) {
+  return (size_t)nslots * nl * pl_of(L, split) * W * sizeof(float2);
 }
-int line_threads(int L, int nl, int W) { return W * m_of(L) * nl; }
+int line_threads(int L, int nl, int W, bool split) { return W * line_m_of(L, split) * nl; }
+int split_override() {
+  static const int v = [] {
+    const char* e = std::getenv("CUPSSGB_SPLIT");
+    return e ? (std::atoi(e) != 0 ? 1 : 0) : -1;
+  }();
+  return v;
+}
+bool turn_split_form(int L, int nl) {
+  (void)nl;
+  if (L < 512) return false;
+  const int o = split_override();
+  return o >= 0 ? o == 1 : true;
+}
 
 cudaError_t launch_line_pass(const LineParams& p, int nl, int nslots, dim3 grid, cudaStream_t st, bool pdl) {
   const size_t smem = line_pass_smem(p.L, nl, p.W, nslots > 0 ? nslots : 1);

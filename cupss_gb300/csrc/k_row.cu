@@ -10,38 +10,50 @@ static bool row_is_one(const XParams& p) {
          p.prod_n[0] >= 1 && p.prod_f[0][0] == 0;
 }
 
-template <int LX>
-static cudaError_t launch_row_t(const XParams& p, cudaStream_t st, int nz, bool pdl) {
-  using C = RowCfg<LX>;
+template <int LX, bool SP>
+static cudaError_t launch_row_form(const XParams& p, cudaStream_t st, int nz, bool pdl) {
+  using C = RowCfg<LX, SP>;
   static bool attr = false, attr_one = false;
   dim3 block(C::M, C::RW);
   dim3 grid((p.rows + C::RW - 1) / C::RW, 1, nz);
   if (row_is_one(p)) {
     const size_t smem = 2 * (size_t)C::RW * C::PL * sizeof(float2);   // two transpose buffers
     if (!attr_one) {
-      cudaError_t e = cudaFuncSetAttribute(row_pass_one<LX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      cudaError_t e = cudaFuncSetAttribute(row_pass_one<LX, SP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            220 * 1024);
       if (e != cudaSuccess) return e;
       attr_one = true;
     }
     LaunchCfg lc(grid, block, smem, st, pdl);
-    return cudaLaunchKernelEx(&lc.cfg, row_pass_one<LX>, p);
+    return cudaLaunchKernelEx(&lc.cfg, row_pass_one<LX, SP>, p);
   }
   const size_t smem = (size_t)(1 + p.n_in) * C::RW * C::PL * sizeof(float2);
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(row_pass<LX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(row_pass<LX, SP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          220 * 1024);
     if (e != cudaSuccess) return e;
     attr = true;
   }
   LaunchCfg lc(grid, block, smem, st, pdl);
-  return cudaLaunchKernelEx(&lc.cfg, row_pass<LX>, p);
+  return cudaLaunchKernelEx(&lc.cfg, row_pass<LX, SP>, p);
+}
+
+// Rows of 512 and 1024 points take the split line FFT (four times / twice the threads
+// per row) when the pass has few rows: a 2D grid has only sy rows, which the four-step
+// form covers with a few warps per SM.  Passes over many rows (3D grids, large batches)
+// keep the four-step form, whose shared-memory traffic is lower.
+static bool row_split(int Lx, long long rows) {
+  if (Lx < 512) return false;
+  const int o = split_override();
+  return o >= 0 ? o == 1 : rows * (long long)line_m_of(Lx, false) < 64LL * 1024;
 }
 
 template <int LX>
-static size_t row_smem_t(int n_in) {
-  using C = RowCfg<LX>;
-  return (size_t)(1 + n_in) * C::RW * C::PL * sizeof(float2);
+static cudaError_t launch_row_t(const XParams& p, cudaStream_t st, int nz, bool pdl) {
+  if constexpr (LX >= 512) {
+    if (row_split(LX, (long long)p.rows * nz)) return launch_row_form<LX, true>(p, st, nz, pdl);
+  }
+  return launch_row_form<LX, false>(p, st, nz, pdl);
 }
 
 cudaError_t launch_row_pass(const XParams& p, cudaStream_t st, int nz, bool pdl) {
@@ -58,23 +70,6 @@ cudaError_t launch_row_pass(const XParams& p, cudaStream_t st, int nz, bool pdl)
     case 512: return launch_row_t<512>(p, st, nz, pdl);
     case 1024: return launch_row_t<1024>(p, st, nz, pdl);
     default: return cudaErrorInvalidValue;
-  }
-}
-
-size_t row_pass_smem(int Lx, int n_in) {
-  switch (Lx) {
-    case 1: return row_smem_t<1>(n_in);
-    case 2: return row_smem_t<2>(n_in);
-    case 4: return row_smem_t<4>(n_in);
-    case 8: return row_smem_t<8>(n_in);
-    case 16: return row_smem_t<16>(n_in);
-    case 32: return row_smem_t<32>(n_in);
-    case 64: return row_smem_t<64>(n_in);
-    case 128: return row_smem_t<128>(n_in);
-    case 256: return row_smem_t<256>(n_in);
-    case 512: return row_smem_t<512>(n_in);
-    case 1024: return row_smem_t<1024>(n_in);
-    default: return 0;
   }
 }
 

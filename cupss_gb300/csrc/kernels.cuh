@@ -75,81 +75,81 @@ __device__ __forceinline__ void static_for(iseq<I...>, F&& f) {
 }
 
 // Twiddle W_sx^k of register I of thread m in the step-2 layout of a packed row
-// (k = m + M (j + J k'), I = j M + k'), from W_sx^m: W_sx^k = W_sx^m W_{2R}^{j + J k'}, the
-// second factor a compile-time constant (sx = 2 R M).  One table load per thread instead
-// of one per register; usable while 2R <= 64 (the compile-time twiddle table).
-template <int LX>
+// (k = m + M c, c = step2_off(I) / M), from W_sx^m: W_sx^k = W_sx^m W_{2R}^c, the second
+// factor a compile-time constant (sx = 2 R M).  One table load per thread instead of one
+// per register; usable while 2R <= 64 (the compile-time twiddle table).
+template <int LX, bool SP>
 struct RowTwSplit {
-  static constexpr bool value = (2 * LineCfg<LX>::R <= 64) && (LineCfg<LX>::M > 1);
+  static constexpr bool value = (2 * LineCfg<LX, SP>::R <= 64) && (LineCfg<LX, SP>::M > 1);
 };
-template <int LX, int I>
+template <int LX, bool SP, int I>
 __device__ __forceinline__ float2 row_twiddle(float2 wm) {
-  constexpr int M = LineCfg<LX>::M, R = LineCfg<LX>::R, J = R / M;
-  return tw_const<2 * R, I / M + J * (I % M), false>(wm);
+  constexpr int M = LineCfg<LX, SP>::M, R = LineCfg<LX, SP>::R;
+  return tw_const<2 * R, step2_off<LX, SP>(I) / M, false>(wm);
 }
 
 // C2R pre-processing of a packed row held in step-2 layout (v) and also stored in T
 // (padded positions): v[i] <- Z at k = pos_step2(m, i), the mirror X[Lx - k] from T.
-template <int LX>
-__device__ __forceinline__ void row_c2r(float2 (&v)[LineCfg<LX>::R], const float2* T, int m, const float2* tw) {
-  constexpr int R = LineCfg<LX>::R, sx = 2 * LX;
-  if constexpr (RowTwSplit<LX>::value) {
+template <int LX, bool SP>
+__device__ __forceinline__ void row_c2r(float2 (&v)[LineCfg<LX, SP>::R], const float2* T, int m, const float2* tw) {
+  constexpr int R = LineCfg<LX, SP>::R, sx = 2 * LX;
+  if constexpr (RowTwSplit<LX, SP>::value) {
     const float2 wm = tw_load(tw, sx, m);
     static_for(make_iseq<R>{}, [&](auto I) {
       constexpr int i = decltype(I)::value;
-      const int k = pos_step2<LX>(m, i);
-      v[i] = c2r_pre_w(v[i], T[pad_pos<LX>((LX - k) & (LX - 1))], k, row_twiddle<LX, i>(wm));
+      const int k = pos_step2<LX, SP>(m, i);
+      v[i] = c2r_pre_w(v[i], T[pad_pos<LX, SP>((LX - k) & (LX - 1))], k, row_twiddle<LX, SP, i>(wm));
     });
   } else {
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      const int k = pos_step2<LX>(m, i);
-      v[i] = c2r_pre(v[i], T[pad_pos<LX>((LX - k) & (LX - 1))], k, sx, tw);
+      const int k = pos_step2<LX, SP>(m, i);
+      v[i] = c2r_pre(v[i], T[pad_pos<LX, SP>((LX - k) & (LX - 1))], k, sx, tw);
     }
   }
 }
 
 // R2C post-processing of a transformed row (v in step-2 layout, also stored in T) and
 // its store to out (packed row).
-template <int LX>
-__device__ __forceinline__ void row_r2c_store(const float2 (&v)[LineCfg<LX>::R], const float2* T, int m,
+template <int LX, bool SP>
+__device__ __forceinline__ void row_r2c_store(const float2 (&v)[LineCfg<LX, SP>::R], const float2* T, int m,
                                               const float2* tw, float2* out, bool live) {
-  constexpr int R = LineCfg<LX>::R, sx = 2 * LX;
-  if constexpr (RowTwSplit<LX>::value) {
+  constexpr int R = LineCfg<LX, SP>::R, sx = 2 * LX;
+  if constexpr (RowTwSplit<LX, SP>::value) {
     const float2 wm = tw_load(tw, sx, m);
     static_for(make_iseq<R>{}, [&](auto I) {
       constexpr int i = decltype(I)::value;
-      const int k = pos_step2<LX>(m, i);
-      const float2 x = r2c_post_w(v[i], T[pad_pos<LX>((LX - k) & (LX - 1))], k, row_twiddle<LX, i>(wm));
+      const int k = pos_step2<LX, SP>(m, i);
+      const float2 x = r2c_post_w(v[i], T[pad_pos<LX, SP>((LX - k) & (LX - 1))], k, row_twiddle<LX, SP, i>(wm));
       if (live) out[k] = x;
     });
   } else {
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      const int k = pos_step2<LX>(m, i);
-      const float2 x = r2c_post(v[i], T[pad_pos<LX>((LX - k) & (LX - 1))], k, sx, tw);
+      const int k = pos_step2<LX, SP>(m, i);
+      const float2 x = r2c_post(v[i], T[pad_pos<LX, SP>((LX - k) & (LX - 1))], k, sx, tw);
       if (live) out[k] = x;
     }
   }
 }
 
-template <int LX>
+template <int LX, bool SP>
 struct RowCfg {
-  static constexpr int M = LineCfg<LX>::M;
-  static constexpr int R = LineCfg<LX>::R;
+  static constexpr int M = LineCfg<LX, SP>::M;
+  static constexpr int R = LineCfg<LX, SP>::R;
   // Padded row length in smem.  A half-warp covers 16/M rows of M threads each
   // (2M banks per row for 8-byte accesses); a pitch = M (mod 16) float2 puts those
   // rows on disjoint banks.
-  static constexpr int PL0 = padded_len<LX>();
+  static constexpr int PL0 = padded_len<LX, SP>();
   static constexpr int PL = (M >= 16) ? PL0 + 1 : PL0 + ((M - PL0 % 16) % 16 + 16) % 16;
   static constexpr int RW = (M >= 128) ? 1 : (128 / M > 32 ? 32 : 128 / M);   // rows per CTA
 };
 
 // smem: (1 + n_in) slots of RW*PL float2.  Slot 0 is the transpose buffer.
-template <int LX>
-__global__ void __launch_bounds__(RowCfg<LX>::M * RowCfg<LX>::RW)
+template <int LX, bool SP>
+__global__ void __launch_bounds__(RowCfg<LX, SP>::M * RowCfg<LX, SP>::RW)
 row_pass(const XParams p) {
-  using C = RowCfg<LX>;
+  using C = RowCfg<LX, SP>;
   constexpr int M = C::M, R = C::R, PL = C::PL, RW = C::RW;
   extern __shared__ float2 smem[];
   grid_dep_sync();
@@ -170,8 +170,8 @@ row_pass(const XParams p) {
       const float2* in = p.in[c] + rowoff;
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        const int n = pos_step1<LX>(m, r);
-        V[pad_pos<LX>(n)] = live ? in[n] : make_float2(0.f, 0.f);
+        const int n = pos_step1<LX, SP>(m, r);
+        V[pad_pos<LX, SP>(n)] = live ? in[n] : make_float2(0.f, 0.f);
       }
       continue;
     }
@@ -180,9 +180,9 @@ row_pass(const XParams p) {
       const float4* in = reinterpret_cast<const float4*>(p.in[c]) + rowoff;
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        const int n = pos_step1<LX>(m, r);
+        const int n = pos_step1<LX, SP>(m, r);
         const float4 q = live ? in[n] : make_float4(0.f, 0.f, 0.f, 0.f);
-        V[pad_pos<LX>(n)] = make_float2(q.x, q.z);
+        V[pad_pos<LX, SP>(n)] = make_float2(q.x, q.z);
       }
       continue;
     }
@@ -193,29 +193,26 @@ row_pass(const XParams p) {
     if (c > 0) __syncthreads();   // CTA-uniform: the previous channel's last reads of T
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      const int k = pos_step2<LX>(m, i);
+      const int k = pos_step2<LX, SP>(m, i);
       v[i] = (live && k < xcols) ? in[k] : make_float2(0.f, 0.f);
-      T[pad_pos<LX>(k)] = v[i];
+      T[pad_pos<LX, SP>(k)] = v[i];
     }
     __syncthreads();
-    row_c2r<LX>(v, T, m, p.tw);
-    inv_step2<LX>(v);
+    row_c2r<LX, SP>(v, T, m, p.tw);
+    inv_step2<LX, SP>(v, m, p.tw);
     __syncthreads();
-#pragma unroll
-    for (int i = 0; i < R; ++i) T[pad_pos<LX>(pos_t2<LX>(m, i))] = v[i];
+    inv_store_t<LX, SP>(v, m, [&](int n, float2 x) { T[pad_pos<LX, SP>(n)] = x; });
     __syncthreads();
+    inv_load_step1<LX, SP>(v, m, p.tw, [&](int n) { return T[pad_pos<LX, SP>(n)]; });
 #pragma unroll
-    for (int s = 0; s < R; ++s) v[s] = T[pad_pos<LX>(pos_t1<LX>(m, s))];
-    inv_step1<LX>(v, m, p.tw);
-#pragma unroll
-    for (int r = 0; r < R; ++r) V[pad_pos<LX>(pos_step1<LX>(m, r))] = v[r];
+    for (int r = 0; r < R; ++r) V[pad_pos<LX, SP>(pos_step1<LX, SP>(m, r))] = v[r];
   }
 
   for (int q = 0; q < p.n_prod; ++q) {
     // pointwise product of the real values (packed as pairs r[2n], r[2n+1])
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      const int a = pad_pos<LX>(pos_step1<LX>(m, r));
+      const int a = pad_pos<LX, SP>(pos_step1<LX, SP>(m, r));
       float2 acc = make_float2(p.out_scale, p.out_scale);   // output scale folded into the product
       for (int t = 0; t < p.prod_n[q]; ++t) {
         float2 x = slot(p.prod_f[q][t])[a];
@@ -228,7 +225,7 @@ row_pass(const XParams p) {
       if (live) {
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-          const int n = pos_step1<LX>(m, r);
+          const int n = pos_step1<LX, SP>(m, r);
           const float2 z = v[r];
           if (p.out_mode == kXOutReal) {
             reinterpret_cast<float2*>(p.out[q])[rowoff + n] = z;
@@ -239,19 +236,17 @@ row_pass(const XParams p) {
       }
       continue;
     }
-    fwd_step1<LX>(v, m, p.tw);
+    fwd_step1<LX, SP>(v, m, p.tw);
     __syncthreads();
 #pragma unroll
-    for (int s = 0; s < R; ++s) T[pad_pos<LX>(pos_t1<LX>(m, s))] = v[s];
+    for (int s = 0; s < R; ++s) T[pad_pos<LX, SP>(pos_t1<LX, SP>(m, s))] = v[s];
+    __syncthreads();
+    fwd_load_step2<LX, SP>(v, m, p.tw, [&](int n) { return T[pad_pos<LX, SP>(n)]; });
     __syncthreads();
 #pragma unroll
-    for (int i = 0; i < R; ++i) v[i] = T[pad_pos<LX>(pos_t2<LX>(m, i))];
-    fwd_step2<LX>(v);
+    for (int i = 0; i < R; ++i) T[pad_pos<LX, SP>(pos_step2<LX, SP>(m, i))] = v[i];
     __syncthreads();
-#pragma unroll
-    for (int i = 0; i < R; ++i) T[pad_pos<LX>(pos_step2<LX>(m, i))] = v[i];
-    __syncthreads();
-    row_r2c_store<LX>(v, T, m, p.tw, reinterpret_cast<float2*>(p.out[q]) + rowoff, live);
+    row_r2c_store<LX, SP>(v, T, m, p.tw, reinterpret_cast<float2*>(p.out[q]) + rowoff, live);
   }
 }
 
@@ -260,16 +255,16 @@ row_pass(const XParams p) {
 // transform directly, so shared memory holds only transpose buffers (no slot for the
 // real-space input) and the input is read once instead of once per factor.  Columns at
 // or beyond in_xcols[0] are known zero (dealiased channel) and are not loaded.
-template <int LX>
+template <int LX, bool SP>
 struct RowOneCfg {
   // resident CTAs per SM the register budget is sized for (RW*M = 128 threads each)
-  static constexpr int kMinBlocks = (LX <= 256) ? 4 : ((LX <= 512) ? 3 : 2);
+  static constexpr int kMinBlocks = (LineCfg<LX, SP>::R <= 16) ? 4 : ((LX <= 512) ? 3 : 2);
 };
 
-template <int LX>
-__global__ void __launch_bounds__(RowCfg<LX>::M * RowCfg<LX>::RW, RowOneCfg<LX>::kMinBlocks)
+template <int LX, bool SP>
+__global__ void __launch_bounds__(RowCfg<LX, SP>::M * RowCfg<LX, SP>::RW, RowOneCfg<LX, SP>::kMinBlocks)
 row_pass_one(const XParams p) {
-  using C = RowCfg<LX>;
+  using C = RowCfg<LX, SP>;
   constexpr int M = C::M, R = C::R, PL = C::PL, RW = C::RW;
   extern __shared__ float2 smem[];
   grid_dep_sync();
@@ -289,19 +284,16 @@ row_pass_one(const XParams p) {
   const float2* in = p.in[0] + rowoff;
 #pragma unroll
   for (int i = 0; i < R; ++i) {
-    const int k = pos_step2<LX>(m, i);
+    const int k = pos_step2<LX, SP>(m, i);
     v[i] = (live && k < xcols) ? in[k] : make_float2(0.f, 0.f);
-    TA[pad_pos<LX>(k)] = v[i];
+    TA[pad_pos<LX, SP>(k)] = v[i];
   }
   __syncthreads();
-  row_c2r<LX>(v, TA, m, p.tw);
-  inv_step2<LX>(v);
-#pragma unroll
-  for (int i = 0; i < R; ++i) TB[pad_pos<LX>(pos_t2<LX>(m, i))] = v[i];
+  row_c2r<LX, SP>(v, TA, m, p.tw);
+  inv_step2<LX, SP>(v, m, p.tw);
+  inv_store_t<LX, SP>(v, m, [&](int n, float2 x) { TB[pad_pos<LX, SP>(n)] = x; });
   __syncthreads();
-#pragma unroll
-  for (int s = 0; s < R; ++s) v[s] = TB[pad_pos<LX>(pos_t1<LX>(m, s))];
-  inv_step1<LX>(v, m, p.tw);
+  inv_load_step1<LX, SP>(v, m, p.tw, [&](int n) { return TB[pad_pos<LX, SP>(n)]; });
   // v[r] = real pair (r[2n], r[2n+1]) at n = m + M r: raise to the product's order
   const int order = p.prod_n[0];
 #pragma unroll
@@ -314,27 +306,25 @@ row_pass_one(const XParams p) {
     }
     v[r] = acc;
   }
-  fwd_step1<LX>(v, m, p.tw);
+  fwd_step1<LX, SP>(v, m, p.tw);
 #pragma unroll
-  for (int s = 0; s < R; ++s) TA[pad_pos<LX>(pos_t1<LX>(m, s))] = v[s];
+  for (int s = 0; s < R; ++s) TA[pad_pos<LX, SP>(pos_t1<LX, SP>(m, s))] = v[s];
   __syncthreads();
+  fwd_load_step2<LX, SP>(v, m, p.tw, [&](int n) { return TA[pad_pos<LX, SP>(n)]; });
 #pragma unroll
-  for (int i = 0; i < R; ++i) v[i] = TA[pad_pos<LX>(pos_t2<LX>(m, i))];
-  fwd_step2<LX>(v);
-#pragma unroll
-  for (int i = 0; i < R; ++i) TB[pad_pos<LX>(pos_step2<LX>(m, i))] = v[i];
+  for (int i = 0; i < R; ++i) TB[pad_pos<LX, SP>(pos_step2<LX, SP>(m, i))] = v[i];
   __syncthreads();
-  row_r2c_store<LX>(v, TB, m, p.tw, reinterpret_cast<float2*>(p.out[0]) + rowoff, live);
+  row_r2c_store<LX, SP>(v, TB, m, p.tw, reinterpret_cast<float2*>(p.out[0]) + rowoff, live);
 }
 
 // ------------------------------------------------------------------------------------
 // line pass (strided axis): forward or inverse FFT of whole lines, in place or not
 // ------------------------------------------------------------------------------------
 // Grid: x = kx' tile (W columns), y = z (kGeoY3) / ky (kGeoZ3).  Block: (W, M, 1).
-// smem: PL * W float2 (one transpose slot).  Lines up to 256 fit the register budget of
-// four resident CTAs per SM (64 registers, no spills), longer ones that of two.
+// smem: PL * W float2 (one transpose slot).  Up to 16 values per thread fit the register
+// budget of four resident CTAs per SM (64 registers, no spills), 32 values that of two.
 template <int L>
-__global__ void __launch_bounds__(256, (L <= 256) ? 4 : 2)
+__global__ void __launch_bounds__(256, (LineCfg<L>::R <= 16) ? 4 : 2)
 line_pass(const LineParams P) {
   constexpr int M = LineCfg<L>::M, R = LineCfg<L>::R;
   extern __shared__ float2 smem[];
@@ -355,9 +345,7 @@ line_pass(const LineParams P) {
 #pragma unroll
       for (int s = 0; s < R; ++s) T[g.sidx(0, pos_t1<L>(g.m, s))] = v[s];
       __syncthreads();
-#pragma unroll
-      for (int i = 0; i < R; ++i) v[i] = T[g.sidx(0, pos_t2<L>(g.m, i))];
-      fwd_step2<L>(v);
+      fwd_load_step2<L>(v, g.m, P.tw, [&](int n) { return T[g.sidx(0, n)]; });
       if (g.ok) {
 #pragma unroll
         for (int i = 0; i < R; ++i) out[g.elem(pos_step2<L>(g.m, i))] = v[i];
@@ -370,14 +358,11 @@ line_pass(const LineParams P) {
         const int nk = (k > L / 2) ? L - k : k;
         v[i] = (g.ok && (keep <= 0 || nk < keep)) ? in[g.elem(k)] : make_float2(0.f, 0.f);
       }
-      inv_step2<L>(v);
+      inv_step2<L>(v, g.m, P.tw);
       if (c > 0) __syncthreads();   // the previous channel's reads of T
-#pragma unroll
-      for (int i = 0; i < R; ++i) T[g.sidx(0, pos_t2<L>(g.m, i))] = v[i];
+      inv_store_t<L>(v, g.m, [&](int n, float2 x) { T[g.sidx(0, n)] = x; });
       __syncthreads();
-#pragma unroll
-      for (int s = 0; s < R; ++s) v[s] = T[g.sidx(0, pos_t1<L>(g.m, s))];
-      inv_step1<L>(v, g.m, P.tw);
+      inv_load_step1<L>(v, g.m, P.tw, [&](int n) { return T[g.sidx(0, n)]; });
       if (g.ok) {
 #pragma unroll
         for (int r = 0; r < R; ++r) out[g.elem(pos_step1<L>(g.m, r))] = v[r];

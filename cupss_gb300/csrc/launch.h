@@ -26,14 +26,21 @@ struct LaunchCfg {
 
 // Row pass over all rows (of nz batch members); picks the template by p.Lx.
 cudaError_t launch_row_pass(const XParams& p, cudaStream_t st, int nz = 1, bool pdl = false);
-size_t row_pass_smem(int Lx, int n_in);
 
 // Line pass: grid.x = ceil(Lx/W) tiles, grid.y per geometry; nl = 2 for the paired
 // 3D z-turnaround.  nslots = shared-memory slots the mode needs.
 cudaError_t launch_line_pass(const LineParams& p, int nl, int nslots, dim3 grid, cudaStream_t st,
                              bool pdl = false);
-size_t line_pass_smem(int L, int nl, int W, int nslots);
-int line_threads(int L, int nl, int W);
+// split: the lines use the split FFT form (LineCfg<L, true>)
+size_t line_pass_smem(int L, int nl, int W, int nslots, bool split = false);
+int line_threads(int L, int nl, int W, bool split = false);
+// The generated turnaround runs lines of 512 and 1024 points in the split form (a 2D grid
+// has only sx/2 such lines; on 3D grids its 16 values per thread leave more warps
+// resident than the four-step form's 32: 512^3 turnaround 1.06 -> 0.78 ms).
+bool turn_split_form(int L, int nl);
+// CUPSSGB_SPLIT=0/1 forces the four-step / split form of lines of 512 and 1024 points in
+// the row pass and the generated turnaround (-1: not set, the automatic choice)
+int split_override();
 
 cudaError_t launch_expand(const ExpandParams& p, cudaStream_t st);
 cudaError_t launch_compress(const CompressParams& p, cudaStream_t st);

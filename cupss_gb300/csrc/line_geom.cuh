@@ -26,9 +26,10 @@ namespace cupssgb {
 // need two updates each (the kx = 0 and kx = sx/2 planes), gets tiles of its own so
 // that no warp mixes it with plain columns: tile index tx = ceil(Lx/W) holds, in thread
 // column w, the pair ty*W + w of column 0; the regular tiles leave column 0 out.
-template <int L, int NL, int WT = 0>
+// SP: the lines use the split FFT form (its padded line length).
+template <int L, int NL, int WT = 0, bool SP = false>
 struct LineGeom {
-  static constexpr int PL = padded_len<L>();
+  static constexpr int PL = padded_len<L, SP>();
   int W, w, m, l, kx0, kxp, lineky;
   int pr;                // NL = 2: pair index of this thread's two lines
   bool packed_tile;      // NL = 2: this CTA works on the packed column kx' = 0
@@ -91,7 +92,7 @@ struct LineGeom {
   __device__ __forceinline__ T* at(T* p) const {
     return p + mbase;
   }
-  __device__ __forceinline__ int sidx(int line, int pos) const { return (line * PL + pad_pos<L>(pos)) * W + w; }
+  __device__ __forceinline__ int sidx(int line, int pos) const { return (line * PL + pad_pos<L, SP>(pos)) * W + w; }
 };
 
 }  // namespace cupssgb

@@ -47,17 +47,17 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 
 // Issues the copies of every state field F reads into its prefetch slots, at the
 // thread's step-2 positions (zeros outside the grid).
-template <int L, class G>
+template <int L, bool SP, class G>
 __device__ __forceinline__ void prefetch_states(const LineParams& P, const FieldK& F, const G& g, float2* smem,
                                                 int n_prod, int slot_sz) {
-  constexpr int R = LineCfg<L>::R;
+  constexpr int R = LineCfg<L, SP>::R;
   const unsigned sbase = smem_u32(smem) + 8u * (unsigned)g.sidx(g.l, 0);
   for (int j = 0; j < F.nsrc; ++j) {
     const unsigned sj = sbase + 8u * (unsigned)((n_prod + j) * slot_sz);
     const float2* st = g.at(P.state[F.src[j]]);
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-      const int pos = pos_step2<L>(g.m, i);
+      const int pos = pos_step2<L, SP>(g.m, i);
       const unsigned off = 8u * (unsigned)(g.sidx(g.l, pos) - g.sidx(g.l, 0));
       cp_async8(sj + off, g.ok ? st + g.elem(pos) : st, g.ok ? 8 : 0);
     }
@@ -137,6 +137,8 @@ struct RtSpec {
   static constexpr int kNProd = -1;   // product channels (-1: P.n_prod)
   static constexpr int kSX = 0, kSY = 0, kSZ = 0;
   static constexpr int kW = 0;   // tile width (0: P.W)
+  // lines of 512 and 1024 points in the split FFT form (more threads per line)
+  static constexpr bool kSplit = false;
   // draw the first field's noise while the first product's loads are in flight (pays off
   // when those loads come from HBM; for grids whose arrays stay in L2 it only delays the
   // transform)
@@ -149,23 +151,30 @@ struct RtSpec {
 // Fourier noise of a thread's R plain modes of one line, drawn in (t, t + Lt/2) pairs
 // (one generator call per pair).
 // The lower registers (positions t < L/2) in order: register of pair p.
-template <int L>
+template <int L, bool SP>
 __host__ __device__ constexpr int lower_reg(int p) {
-  constexpr int Mx = LineCfg<L>::M;
-  return (L == 1) ? 0 : ((Mx >= 2) ? (p / (Mx / 2)) * Mx + p % (Mx / 2) : p);
+  constexpr int Mx = LineCfg<L, SP>::M;
+  if (L == 1) return 0;
+  if (LineCfg<L, SP>::kSplit || Mx < 2) return p;
+  return (p / (Mx / 2)) * Mx + p % (Mx / 2);
+}
+// Register offset of position t + L/2 from the register of position t.
+template <int L, bool SP>
+__host__ __device__ constexpr int upper_half_reg() {
+  constexpr int Mx = LineCfg<L, SP>::M;
+  return (LineCfg<L, SP>::kSplit || Mx < 2) ? LineCfg<L, SP>::R / 2 : Mx / 2;
 }
 
-template <int L>
+template <int L, bool SP>
 __device__ __forceinline__ void draw_line_noise(const LineParams& P, const NoiseKey& nk, int fid, const LinePre& lp,
-                                                float2 (&xi)[LineCfg<L>::R]) {
-  constexpr int R = LineCfg<L>::R;
-  constexpr int Mx = LineCfg<L>::M;
-  constexpr int HALF = (Mx >= 2) ? Mx / 2 : R / 2;   // register offset of t + L/2
+                                                float2 (&xi)[LineCfg<L, SP>::R]) {
+  constexpr int R = LineCfg<L, SP>::R;
+  constexpr int HALF = upper_half_reg<L, SP>();   // register offset of t + L/2
   constexpr int NP = (L == 1) ? 1 : R / 2;            // generator calls: one per pair
   uint32_t c[NP][4];
 #pragma unroll
   for (int q = 0; q < NP; ++q) {
-    c[q][0] = lp.lin0 + (uint32_t)pos_step2<L>(0, lower_reg<L>(q)) * lp.lin_step;
+    c[q][0] = lp.lin0 + (uint32_t)pos_step2<L, SP>(0, lower_reg<L, SP>(q)) * lp.lin_step;
     c[q][1] = nk.step;
     c[q][2] = (uint32_t)fid;
     c[q][3] = 0u;
@@ -173,7 +182,7 @@ __device__ __forceinline__ void draw_line_noise(const LineParams& P, const Noise
   philox4x32_10_batch<NP>(c, nk.key0, nk.key1);
 #pragma unroll
   for (int q = 0; q < NP; ++q) {
-    const int i = lower_reg<L>(q);
+    const int i = lower_reg<L, SP>(q);
     float g1, g2, g3, g4;
     box_muller(c[q][0], c[q][1], g1, g2);
     box_muller(c[q][2], c[q][3], g3, g4);
@@ -183,12 +192,12 @@ __device__ __forceinline__ void draw_line_noise(const LineParams& P, const Noise
 }
 
 // keep_fixed: the dealias test of the axes other than the line axis (per thread and field).
-template <int L, bool Z3, class Prog, class G>
+template <int L, bool SP, bool Z3, class Prog, class G>
 __device__ __forceinline__ float2 update_mode(const LineParams& P, const LinePre& lp, const FieldK& F, int fi,
                                               const G& g, int i, const float2* smem, int n_prod, bool has_chan,
                                               bool keep_fixed, float2 xi, bool p0_reg = false,
                                               float2 p0 = float2{0.f, 0.f}) {
-  const int C = pos_step2<L>(0, i);
+  const int C = pos_step2<L, SP>(0, i);
   const int pos = g.m + C;
   Fetch fx;
   fx.smem = smem;
@@ -209,7 +218,8 @@ __device__ __forceinline__ float2 update_mode(const LineParams& P, const LinePre
 
 template <int L, int NL, class Prog, class Spec = RtSpec>
 __device__ __forceinline__ void turn_body(const LineParams& P) {
-  constexpr int R = LineCfg<L>::R;
+  constexpr bool SP = Spec::kSplit;
+  constexpr int R = LineCfg<L, SP>::R;
   constexpr bool Z3 = (NL == 2);   // the paired z-line form is the 3D turnaround
   extern __shared__ float2 smem[];
   grid_dep_sync();
@@ -220,7 +230,7 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
     nk = NoiseKey{mk.key0, mk.key1, mk.step + P.step_off};
   }
   const Dims d = Spec::kSX ? Dims{Spec::kSX, Spec::kSY, Spec::kSZ} : dims_of(P);
-  const LineGeom<L, NL, Spec::kW> g(P, d.sy, d.sx / 2);
+  const LineGeom<L, NL, Spec::kW, SP> g(P, d.sy, d.sx / 2);
   if (g.idle) return;   // CTA-uniform, before any barrier
   const int m = g.m, l = g.l;
   const int slot_sz = g.slot_sz;
@@ -231,7 +241,7 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
 
   // 0) the states the first field reads start on their way to shared memory now, and
   //    arrive while the products are transformed
-  if (nf > 0) prefetch_states<L>(P, P.f[0], g, smem, n_prod, slot_sz);
+  if (nf > 0) prefetch_states<L, SP>(P, P.f[0], g, smem, n_prod, slot_sz);
 
   // 1) forward transform of every product channel into its slot (step-2 positions).
   //    The first field's Fourier noise depends on no data: with a generated program it is
@@ -243,12 +253,12 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
   auto load_product = [&](int c) {
     const float2* in = g.at(P.prod_in[c]);
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = g.ok ? in[g.elem(pos_step1<L>(m, r))] : make_float2(0.f, 0.f);
+    for (int r = 0; r < R; ++r) v[r] = g.ok ? in[g.elem(pos_step1<L, SP>(m, r))] : make_float2(0.f, 0.f);
   };
   if (n_prod > 0) load_product(0);
   if constexpr (Prog::kUnroll && Spec::kEarlyNoise) {
     if (nf > 0 && plain && P.f[0].noisy)
-      draw_line_noise<L>(P, nk, P.f[0].fid, line_pre<Z3>(P, d, g.kxp, g.lineky, m), xi0);
+      draw_line_noise<L, SP>(P, nk, P.f[0].fid, line_pre<Z3>(P, d, g.kxp, g.lineky, m), xi0);
   }
   // One field and one product (the Cahn-Hilliard form): the transformed product stays in
   // v, at the modes the thread updates, unless a thread of the CTA reads a Hermitian
@@ -257,17 +267,15 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
   for (int c = 0; c < n_prod; ++c) {
     float2* Sl = smem + c * slot_sz;
     if (c > 0) load_product(c);
-    fwd_step1<L>(v, m, P.tw);
+    fwd_step1<L, SP>(v, m, P.tw);
 #pragma unroll
-    for (int s = 0; s < R; ++s) Sl[g.sidx(l, pos_t1<L>(m, s))] = v[s];
+    for (int s = 0; s < R; ++s) Sl[g.sidx(l, pos_t1<L, SP>(m, s))] = v[s];
     __syncthreads();
-#pragma unroll
-    for (int i = 0; i < R; ++i) v[i] = Sl[g.sidx(l, pos_t2<L>(m, i))];
-    fwd_step2<L>(v);
+    fwd_load_step2<L, SP>(v, m, P.tw, [&](int n) { return Sl[g.sidx(l, n)]; });
     if (p0_reg) break;   // the only product: kept in v
     __syncthreads();
 #pragma unroll
-    for (int i = 0; i < R; ++i) Sl[g.sidx(l, pos_step2<L>(m, i))] = v[i];
+    for (int i = 0; i < R; ++i) Sl[g.sidx(l, pos_step2<L, SP>(m, i))] = v[i];
   }
 
   auto field_step = [&](const int fi) {
@@ -297,11 +305,11 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
 #pragma unroll
           for (int i = 0; i < R; ++i) ch[i] = xi0[i];
         } else if (F.noisy) {
-          draw_line_noise<L>(P, nk, F.fid, lp, ch);
+          draw_line_noise<L, SP>(P, nk, F.fid, lp, ch);
         }
 #pragma unroll
         for (int i = 0; i < R; ++i)
-          ch[i] = update_mode<L, Z3, Prog>(P, lp, F, fi, g, i, smem, n_prod, has_chan, keep_fixed, ch[i], p0_reg,
+          ch[i] = update_mode<L, SP, Z3, Prog>(P, lp, F, fi, g, i, smem, n_prod, has_chan, keep_fixed, ch[i], p0_reg,
                                            v[i]);
       } else {
         // table-driven program: a rolled loop (its unrolled code would be very large);
@@ -311,10 +319,10 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
         for (int i = 0; i < R; ++i) {
           float2 xi = make_float2(0.f, 0.f);
           if (F.noisy) {
-            const int pos = pos_step2<L>(m, i);
+            const int pos = pos_step2<L, SP>(m, i);
             xi = Z3 ? noise_at(P, d, nk, F.fid, g.kxp, g.lineky, pos) : noise_at(P, d, nk, F.fid, g.kxp, pos, 0);
           }
-          chl[i] = update_mode<L, Z3, Prog>(P, lp, F, fi, g, i, smem, n_prod, has_chan, keep_fixed, xi);
+          chl[i] = update_mode<L, SP, Z3, Prog>(P, lp, F, fi, g, i, smem, n_prod, has_chan, keep_fixed, xi);
         }
 #pragma unroll
         for (int i = 0; i < R; ++i) ch[i] = chl[i];
@@ -326,7 +334,7 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
       float2 chl[R];
 #pragma unroll 1
       for (int i = 0; i < R; ++i) {
-        const int pos = pos_step2<L>(m, i);
+        const int pos = pos_step2<L, SP>(m, i);
         const int ky = Z3 ? g.lineky : pos;
         const int kz = Z3 ? pos : 0;
         const int ppos = (L - pos) & (L - 1);
@@ -362,19 +370,16 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
       if (g.pr > 0 && g.pr > F.chan_ylimit) skip = true;
     }
     __syncthreads();   // every read of the slots is done
-    if (fi + 1 < nf) prefetch_states<L>(P, P.f[fi + 1], g, smem, n_prod, slot_sz);
+    if (fi + 1 < nf) prefetch_states<L, SP>(P, P.f[fi + 1], g, smem, n_prod, slot_sz);
     if (skip) return;   // CTA-uniform: masked tile, the channel stays zero
     float2* Ts = smem + P.tslot * slot_sz;
-    inv_step2<L>(ch);
-#pragma unroll
-    for (int i = 0; i < R; ++i) Ts[g.sidx(l, pos_t2<L>(m, i))] = ch[i];
+    inv_step2<L, SP>(ch, m, P.tw);
+    inv_store_t<L, SP>(ch, m, [&](int n, float2 x) { Ts[g.sidx(l, n)] = x; });
     __syncthreads();
-#pragma unroll
-    for (int s = 0; s < R; ++s) ch[s] = Ts[g.sidx(l, pos_t1<L>(m, s))];
-    inv_step1<L>(ch, m, P.tw);
+    inv_load_step1<L, SP>(ch, m, P.tw, [&](int n) { return Ts[g.sidx(l, n)]; });
     if (g.ok) {
 #pragma unroll
-      for (int r = 0; r < R; ++r) g.at(F.chan)[g.elem(pos_step1<L>(m, r))] = ch[r];
+      for (int r = 0; r < R; ++r) g.at(F.chan)[g.elem(pos_step1<L, SP>(m, r))] = ch[r];
     }
     // the next field writes Ts only after its update and the barrier that follows it,
     // which every thread reaches after its reads of Ts above

@@ -158,8 +158,10 @@ def test_kpz_2d_with_nondynamic_fields():
         assert err < 3e-5, (n, err)
 
 
-def test_model_h_2d():
-    shape = (32, 32, 1)
+@pytest.mark.parametrize("shape", [(32, 32, 1), (1024, 16, 1), (16, 1024, 1), (32, 512, 1)])
+def test_model_h_2d(shape):
+    """Model H, 6 fields.  The long-line shapes run the split line FFT (512 and 1024
+    points) in the multi-input row pass and in the multi-field turnaround."""
     spec = ([("phi", 1), ("iqxphi", 0), ("iqyphi", 0), ("lapphi", 0), ("vx", 0), ("vy", 0)],
             {"a": -1.0, "b": 1.0, "k": 4.0, "eta": 1.0, "T": 0.001},
             ["dt phi + q^2*(a + k*q^2)*phi = -b*q^2*phi^3 - vx*iqxphi - vy*iqyphi",
@@ -290,7 +292,8 @@ def test_edwards_wilkinson_stationary_spectrum():
 
 
 @pytest.mark.parametrize("shape", [(2, 1, 1), (4, 1, 1), (8, 1, 1), (2048, 1, 1), (4, 2, 1), (16, 1024, 1),
-                                   (1024, 4, 1), (4, 4, 2), (8, 2, 1024), (4, 256, 8), (512, 2, 4)])
+                                   (1024, 4, 1), (4, 4, 2), (8, 2, 1024), (4, 256, 8), (512, 2, 4),
+                                   (4, 512, 4), (8, 4, 512), (4, 1024, 2), (2048, 2, 2)])
 def test_fft_sizes_round_trip_and_one_step(shape):
     import cupss_gb300 as c
     sx, sy, sz = shape

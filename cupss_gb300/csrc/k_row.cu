@@ -28,14 +28,19 @@ static cudaError_t launch_row_form(const XParams& p, cudaStream_t st, int nz, bo
     return cudaLaunchKernelEx(&lc.cfg, row_pass_one<LX, SP>, p);
   }
   const size_t smem = (size_t)(1 + p.n_in) * C::RW * C::PL * sizeof(float2);
+  void (*kern)(const XParams) = nullptr;
+  if constexpr (SP) {
+    kern = row_pass_split<LX>;
+  } else {
+    kern = row_pass<LX>;
+  }
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(row_pass<LX, SP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         220 * 1024);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     if (e != cudaSuccess) return e;
     attr = true;
   }
   LaunchCfg lc(grid, block, smem, st, pdl);
-  return cudaLaunchKernelEx(&lc.cfg, row_pass<LX, SP>, p);
+  return cudaLaunchKernelEx(&lc.cfg, kern, p);
 }
 
 // Rows of 512 and 1024 points take the split line FFT (four times / twice the threads

@@ -147,8 +147,7 @@ struct RowCfg {
 
 // smem: (1 + n_in) slots of RW*PL float2.  Slot 0 is the transpose buffer.
 template <int LX, bool SP>
-__global__ void __launch_bounds__(RowCfg<LX, SP>::M * RowCfg<LX, SP>::RW)
-row_pass(const XParams p) {
+__device__ __forceinline__ void row_pass_body(const XParams& p) {
   using C = RowCfg<LX, SP>;
   constexpr int M = C::M, R = C::R, PL = C::PL, RW = C::RW;
   extern __shared__ float2 smem[];
@@ -163,6 +162,29 @@ row_pass(const XParams p) {
   auto slot = [&](int i) { return smem + (size_t)(1 + i) * RW * PL + rl * PL; };
   const size_t rowoff = (size_t)blockIdx.z * p.mstride + (size_t)(live ? row : 0) * LX;
   float2 v[R];
+
+  // Spectral inputs: every channel's row is copied into its slot asynchronously at once,
+  // so that the loads of all channels are in flight together; each channel's inverse
+  // transform then reads its row, and the Hermitian mirror X[Lx - k] of the C2R step,
+  // from the slot, and finally overwrites the slot with its real-space values.
+  const bool spectral = p.in_mode == kXInSpectral;
+  if (spectral) {
+#pragma unroll 1
+    for (int c = 0; c < p.n_in; ++c) {
+      const float2* in = p.in[c] + rowoff;
+      const int xcols = p.in_xcols[c] > 0 ? p.in_xcols[c] : LX;
+      const unsigned sv = smem_u32(slot(c));
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        const int k = pos_step2<LX, SP>(m, i);
+        const bool ld = live && k < xcols;   // columns at or beyond xcols are known zero
+        cp_async8(sv + 8u * (unsigned)pad_pos<LX, SP>(k), ld ? in + k : in, ld ? 8 : 0);
+      }
+    }
+    cp_async_commit();
+    cp_async_wait_all();
+    __syncthreads();
+  }
 
   for (int c = 0; c < p.n_in; ++c) {
     float2* V = slot(c);
@@ -186,21 +208,14 @@ row_pass(const XParams p) {
       }
       continue;
     }
-    const float2* in = p.in[c] + rowoff;
-    const int xcols = p.in_xcols[c] > 0 ? p.in_xcols[c] : LX;
-    // the row goes through the transpose buffer once so that the mirrored element
-    // X[Lx - k] of the C2R pre-processing comes from shared memory
-    if (c > 0) __syncthreads();   // CTA-uniform: the previous channel's last reads of T
+    // the staged spectral row (every thread's copies are complete and visible: wait and
+    // barrier above); the slot is overwritten only after the two barriers below, which
+    // follow every thread's reads of it
 #pragma unroll
-    for (int i = 0; i < R; ++i) {
-      const int k = pos_step2<LX, SP>(m, i);
-      v[i] = (live && k < xcols) ? in[k] : make_float2(0.f, 0.f);
-      T[pad_pos<LX, SP>(k)] = v[i];
-    }
-    __syncthreads();
-    row_c2r<LX, SP>(v, T, m, p.tw);
+    for (int i = 0; i < R; ++i) v[i] = V[pad_pos<LX, SP>(pos_step2<LX, SP>(m, i))];
+    row_c2r<LX, SP>(v, V, m, p.tw);
     inv_step2<LX, SP>(v, m, p.tw);
-    __syncthreads();
+    __syncthreads();   // CTA-uniform: the previous channel's last reads of T
     inv_store_t<LX, SP>(v, m, [&](int n, float2 x) { T[pad_pos<LX, SP>(n)] = x; });
     __syncthreads();
     inv_load_step1<LX, SP>(v, m, p.tw, [&](int n) { return T[pad_pos<LX, SP>(n)]; });
@@ -248,6 +263,17 @@ row_pass(const XParams p) {
     __syncthreads();
     row_r2c_store<LX, SP>(v, T, m, p.tw, reinterpret_cast<float2*>(p.out[q]) + rowoff, live);
   }
+}
+
+// The four-step form and the split form (register budget of two resident CTAs per SM:
+// without it the register allocation of the split form spills).
+template <int LX>
+__global__ void __launch_bounds__(RowCfg<LX, false>::M * RowCfg<LX, false>::RW) row_pass(const XParams p) {
+  row_pass_body<LX, false>(p);
+}
+template <int LX>
+__global__ void __launch_bounds__(RowCfg<LX, true>::M * RowCfg<LX, true>::RW, 2) row_pass_split(const XParams p) {
+  row_pass_body<LX, true>(p);
 }
 
 // Single spectral input, single spectral product (the Cahn-Hilliard form phi^n): the

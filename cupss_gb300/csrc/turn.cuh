@@ -31,20 +31,6 @@
 
 namespace cupssgb {
 
-// 32-bit shared-window address of a shared-memory pointer.
-__device__ __forceinline__ unsigned smem_u32(const void* p) {
-  unsigned sa;
-  asm("{ .reg .u64 t; cvta.to.shared.u64 t, %1; cvt.u32.u64 %0, t; }" : "=r"(sa) : "l"(p));
-  return sa;
-}
-// 8-byte asynchronous global -> shared copy to shared address sa (zero-filled when
-// src_bytes is 0, in which case nothing is read).
-__device__ __forceinline__ void cp_async8(unsigned sa, const float2* gsrc, int src_bytes) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(sa), "l"(gsrc), "r"(src_bytes) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
-
 // Issues the copies of every state field F reads into its prefetch slots, at the
 // thread's step-2 positions (zeros outside the grid).
 template <int L, bool SP, class G>

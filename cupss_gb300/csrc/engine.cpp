@@ -286,7 +286,7 @@ static int sm_count() {
 }
 
 bool Solver::turn_split() const {
-  return use_jit_ && turn_split_form(dim_ == 3 ? sz_ : sy_, dim_ == 3 ? 2 : 1);
+  return use_jit_ && turn_split_form(dim_ == 3 ? sz_ : sy_);
 }
 
 int Solver::pick_w(int L, int nl, int nslots, int other, bool split) const {

@@ -71,7 +71,7 @@ std::string jit_generate_turn(const LineParams& p, int L, int NL, int warps, boo
                    : "P.f[" + std::to_string(fi) + "].noise_base";
   };
   // block = (W, M, NL) threads
-  const bool split = turn_split_form(L, NL);
+  const bool split = turn_split_form(L);
   const int M = line_threads(L, 1, 1, split);   // LineCfg<L, split>::M
   const int threads = p.W > 0 ? p.W * M * NL : 256;
   const int min_blocks = std::max(1, warps * 32 / threads);

@@ -22,11 +22,10 @@ int split_override() {
   }();
   return v;
 }
-bool turn_split_form(int L, int nl) {
-  (void)nl;
+bool turn_split_form(int L) {
   if (L < 512) return false;
   const int o = split_override();
-  return o >= 0 ? o == 1 : true;
+  return o < 0 || o == 1;   // automatic: the split form
 }
 
 cudaError_t launch_line_pass(const LineParams& p, int nl, int nslots, dim3 grid, cudaStream_t st, bool pdl) {

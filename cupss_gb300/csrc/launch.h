@@ -37,7 +37,7 @@ int line_threads(int L, int nl, int W, bool split = false);
 // The generated turnaround runs lines of 512 and 1024 points in the split form (a 2D grid
 // has only sx/2 such lines; on 3D grids its 16 values per thread leave more warps
 // resident than the four-step form's 32: 512^3 turnaround 1.06 -> 0.78 ms).
-bool turn_split_form(int L, int nl);
+bool turn_split_form(int L);
 // CUPSSGB_SPLIT=0/1 forces the four-step / split form of lines of 512 and 1024 points in
 // the row pass and the generated turnaround (-1: not set, the automatic choice)
 int split_override();

@@ -92,3 +92,18 @@ def test_server_declaration_errors(built_lib):
     with pytest.raises(c.CupssError):
         srv.submit(sid, (32, 32, 1), 0.01, 0)
     srv.close()
+
+
+@pytest.mark.parametrize("shape,split", [((64, 1024, 1), True), ((64, 512, 1), True), ((64, 256, 1), False),
+                                         ((8, 8, 512), True), ((8, 8, 256), False)])
+def test_turnaround_line_form(built_lib, shape, split):
+    """Lines of 512 and 1024 points along the turnaround axis are generated in the split
+    FFT form, shorter ones in the four-step form."""
+    from cupss_gb300.api import jit_check
+    from tests.test_parser_parity import build_lib
+    ir = build_lib([("phi", 1)], {"a": -1.0, "b": 1.0, "k": 1.0, "T": 0.01},
+                   ["dt phi + q^2*(a + k*q^2)*phi = -b*q^2*phi^3"], [("phi", "2*T*q^2")])
+    s = solver_from_ir(ir, shape)
+    (src,) = s.generated_sources()
+    assert ("kSplit = %s;" % ("true" if split else "false")) in src
+    assert jit_check(src) > 0

@@ -107,3 +107,22 @@ def test_turnaround_line_form(built_lib, shape, split):
     (src,) = s.generated_sources()
     assert ("kSplit = %s;" % ("true" if split else "false")) in src
     assert jit_check(src) > 0
+
+
+def test_member_memory_estimate(built_lib):
+    """The device bytes a batch would allocate (the server's HBM-budget admission uses
+    them): linear in the members, and at least the spectra a member needs: two states and
+    one dealiased channel for phi, one product, 4 B per grid point each (packed half
+    spectra)."""
+    from tests.test_parser_parity import build_lib
+    ir = build_lib([("phi", 1)], {"a": -1.0, "b": 1.0, "k": 1.0},
+                   ["dt phi + q^2*(a + k*q^2)*phi = -b*q^2*phi^3"], [])
+    for shape in ((64, 64, 1), (32, 16, 8)):
+        s = solver_from_ir(ir, shape)
+        e = [s.estimate_bytes(m) for m in (2, 3, 4, 8)]
+        per = e[1] - e[0]
+        assert e[2] - e[1] == per and e[3] - e[2] == 4 * per
+        npts = shape[0] * shape[1] * shape[2]
+        assert per >= 4 * 4 * npts
+        assert s.estimate_bytes(1) > 0
+        s.close()

@@ -215,6 +215,24 @@ def set_device(dev):
     capi.check(capi.load().cupssgb_set_device(int(dev)))
 
 
+def device_info():
+    """(number of visible CUDA devices, one text line per device plus the versions)."""
+    lib = capi.load()
+    buf = C.create_string_buffer(8192)
+    n = lib.cupssgb_device_info(buf, len(buf))
+    if n < 0:
+        capi.check(n)
+    return n, buf.value.decode()
+
+
+def write_field_csv(path, name, values, precision=6):
+    """One field file in the reference's CSV format; values shaped (sz, sy, sx) or (sy, sx) or (sx,)."""
+    a = np.ascontiguousarray(np.asarray(values, np.float32))
+    shp = a.shape[::-1] + (1,) * (3 - a.ndim)
+    return capi.check(capi.load().cupssgb_write_field_csv(str(path).encode(), name.encode(), capi.fptr(a.reshape(-1)),
+                                                          shp[0], shp[1], shp[2], int(precision)))
+
+
 class Evolver:
     """Mirror of the reference ``evolver`` (same method names as the C++ API)."""
 
@@ -288,6 +306,45 @@ class Evolver:
 
     def getCurrentTimestep(self):
         return self.lib.cupssgb_evolver_current_step(self.h)
+
+    def flushOutput(self):
+        return capi.check(self.lib.cupssgb_evolver_flush_output(self.h))
+
+    def createFromFile(self, path):
+        return capi.check(self.lib.cupssgb_evolver_create_from_file(self.h, str(path).encode()))
+
+    def initializeUniform(self, name, value):
+        return capi.check(self.lib.cupssgb_evolver_initialize_uniform(self.h, name.encode(), float(value)))
+
+    def initializeUniformNoise(self, name, amplitude):
+        return capi.check(self.lib.cupssgb_evolver_initialize_uniform_noise(self.h, name.encode(), float(amplitude)))
+
+    def initializeNormalNoise(self, name, mean, sigma):
+        return capi.check(self.lib.cupssgb_evolver_initialize_normal_noise(self.h, name.encode(), float(mean),
+                                                                           float(sigma)))
+
+    def initializeHalfSystem(self, name, value1, value2, width, direction):
+        return capi.check(self.lib.cupssgb_evolver_initialize_half_system(self.h, name.encode(), float(value1),
+                                                                          float(value2), float(width), int(direction)))
+
+    def initializeDroplet(self, name, value_out, value_in, radius, width, cx, cy, cz):
+        return capi.check(self.lib.cupssgb_evolver_initialize_droplet(self.h, name.encode(), float(value_out),
+                                                                      float(value_in), float(radius), float(width),
+                                                                      int(cx), int(cy), int(cz)))
+
+    def addDroplet(self, name, value, radius, width, cx, cy, cz):
+        return capi.check(self.lib.cupssgb_evolver_add_droplet(self.h, name.encode(), float(value), float(radius),
+                                                               float(width), int(cx), int(cy), int(cz)))
+
+    def initializeFromFile(self, name, path, skiprows=0, delimiter=","):
+        return capi.check(self.lib.cupssgb_evolver_initialize_from_file(self.h, name.encode(), str(path).encode(),
+                                                                        int(skiprows), delimiter.encode()))
+
+    def getHostReal(self, name):
+        """The host array of a field (fieldsReal): what the initializers or setReal wrote."""
+        out = np.empty(self.N, np.float32)
+        capi.check(self.lib.cupssgb_evolver_get_host_real(self.h, name.encode(), capi.fptr(out)))
+        return out.reshape(self.shape)
 
     def setCallback(self, name, fn, fourier=False):
         """fn(evolver_ptr, field_ptr, sx, sy, sz) -> None, or None to remove.  The ctypes

@@ -103,6 +103,19 @@ SIGNATURES = {
     "cupssgb_host_alloc": (_I, [_LL, C.POINTER(_P)]),
     "cupssgb_host_free": (_I, [_P]),
     "cupssgb_set_device": (_I, [_I]),
+    "cupssgb_device_info": (_I, [C.c_char_p, _I]),
+    "cupssgb_solver_snapshot_real": (_I, [_P, _I, _P, _P]),
+    "cupssgb_evolver_flush_output": (_I, [_P]),
+    "cupssgb_evolver_create_from_file": (_I, [_P, _S]),
+    "cupssgb_evolver_initialize_uniform": (_I, [_P, _S, _F]),
+    "cupssgb_evolver_initialize_uniform_noise": (_I, [_P, _S, _F]),
+    "cupssgb_evolver_initialize_normal_noise": (_I, [_P, _S, _F, _F]),
+    "cupssgb_evolver_initialize_half_system": (_I, [_P, _S, _F, _F, _F, _I]),
+    "cupssgb_evolver_initialize_droplet": (_I, [_P, _S, _F, _F, _F, _F, _I, _I, _I]),
+    "cupssgb_evolver_add_droplet": (_I, [_P, _S, _F, _F, _F, _I, _I, _I]),
+    "cupssgb_evolver_initialize_from_file": (_I, [_P, _S, _S, _I, C.c_char]),
+    "cupssgb_evolver_get_host_real": (_I, [_P, _S, _FP]),
+    "cupssgb_write_field_csv": (_I, [_S, _S, _FP, _I, _I, _I, _I]),
     "cupssgb_evolver_create": (_I, [_I, _I, _I, _I, _F, _F, _F, _F, _I, C.POINTER(_P)]),
     "cupssgb_evolver_destroy": (_I, [_P]),
     "cupssgb_evolver_create_field": (_I, [_P, _S, _I]),

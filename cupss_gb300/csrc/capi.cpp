@@ -390,9 +390,42 @@ int cupssgb_host_free(void* p) {
   return e == cudaSuccess ? 0 : fail(CUPSSGB_ERR_CUDA, cudaGetErrorString(e));
 }
 
+int cupssgb_solver_snapshot_real(cupssgb_solver* s, int field, float* host_real, void* done_event) {
+  NEED(s);
+  return guard([&] {
+    s->s->snapshot_real(field, host_real, (cudaEvent_t)done_event);
+    return 0;
+  });
+}
+
 int cupssgb_set_device(int device) {
   cudaError_t e = cudaSetDevice(device);
   return e == cudaSuccess ? 0 : fail(CUPSSGB_ERR_CUDA, cudaGetErrorString(e));
+}
+
+int cupssgb_device_info(char* buf, int buflen) {
+  int n = 0, drv = 0, rt = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) {
+    cudaGetLastError();
+    n = 0;
+  } else if (e != cudaSuccess) {
+    return fail(CUPSSGB_ERR_CUDA, std::string("cudaGetDeviceCount: ") + cudaGetErrorString(e));
+  }
+  std::ostringstream os;
+  for (int i = 0; i < n; ++i) {
+    cudaDeviceProp pr;
+    e = cudaGetDeviceProperties(&pr, i);
+    if (e != cudaSuccess) return fail(CUPSSGB_ERR_CUDA, std::string("cudaGetDeviceProperties: ") + cudaGetErrorString(e));
+    os << i << ": " << pr.name << ", " << pr.multiProcessorCount << " SMs, sm_" << pr.major << pr.minor << ", "
+       << (pr.totalGlobalMem >> 20) << " MiB\n";
+  }
+  cudaDriverGetVersion(&drv);
+  cudaRuntimeGetVersion(&rt);
+  os << "driver " << drv / 1000 << "." << (drv % 1000) / 10 << ", runtime " << rt / 1000 << "." << (rt % 1000) / 10
+     << "\n";
+  copy_out(os.str(), buf, buflen);
+  return n;
 }
 
 long long cupssgb_solver_step_count(const cupssgb_solver* s) { return s ? s->s->step_count() : -1; }
@@ -514,6 +547,86 @@ int cupssgb_evolver_write_out(cupssgb_evolver* e) {
   return guard([&] {
     e->e->writeOut();
     return 0;
+  });
+}
+
+int cupssgb_evolver_flush_output(cupssgb_evolver* e) {
+  NEED(e);
+  return guard([&] {
+    e->e->flushOutput();
+    return 0;
+  });
+}
+
+int cupssgb_evolver_create_from_file(cupssgb_evolver* e, const char* path) {
+  NEED(e);
+  NEED(path);
+  return guard([&] {
+    const int r = e->e->createFromFile(path);
+    return r == 0 ? 0 : fail(CUPSSGB_ERR_PARSE, std::string("cannot read system file ") + path);
+  });
+}
+
+#define CUPSSGB_INIT_CALL(call)                                                               \
+  NEED(e);                                                                                    \
+  NEED(name);                                                                                 \
+  return guard([&] {                                                                          \
+    if (!find_field(e->e, name)) return fail(CUPSSGB_ERR_INVALID, std::string("no field ") + name); \
+    e->e->call;                                                                               \
+    return 0;                                                                                 \
+  })
+
+int cupssgb_evolver_initialize_uniform(cupssgb_evolver* e, const char* name, float value) {
+  CUPSSGB_INIT_CALL(initializeUniform(name, value));
+}
+int cupssgb_evolver_initialize_uniform_noise(cupssgb_evolver* e, const char* name, float amplitude) {
+  CUPSSGB_INIT_CALL(initializeUniformNoise(name, amplitude));
+}
+int cupssgb_evolver_initialize_normal_noise(cupssgb_evolver* e, const char* name, float mean, float sigma) {
+  CUPSSGB_INIT_CALL(initializeNormalNoise(name, mean, sigma));
+}
+int cupssgb_evolver_initialize_half_system(cupssgb_evolver* e, const char* name, float value1, float value2,
+                                           float interface_width, int direction) {
+  CUPSSGB_INIT_CALL(initializeHalfSystem(name, value1, value2, interface_width, direction));
+}
+int cupssgb_evolver_initialize_droplet(cupssgb_evolver* e, const char* name, float value_out, float value_in,
+                                       float radius, float interface_width, int center_x, int center_y,
+                                       int center_z) {
+  CUPSSGB_INIT_CALL(initializeDroplet(name, value_out, value_in, radius, interface_width, center_x, center_y, center_z));
+}
+int cupssgb_evolver_add_droplet(cupssgb_evolver* e, const char* name, float value, float radius,
+                                float interface_width, int center_x, int center_y, int center_z) {
+  CUPSSGB_INIT_CALL(addDroplet(name, value, radius, interface_width, center_x, center_y, center_z));
+}
+int cupssgb_evolver_initialize_from_file(cupssgb_evolver* e, const char* name, const char* path, int skiprows,
+                                         char delimiter) {
+  NEED(path);
+  CUPSSGB_INIT_CALL(initializeFromFile(name, path, skiprows, delimiter));
+}
+#undef CUPSSGB_INIT_CALL
+
+int cupssgb_evolver_get_host_real(cupssgb_evolver* e, const char* name, float* host_real) {
+  NEED(e);
+  NEED(host_real);
+  return guard([&] {
+    field* f = find_field(e->e, name);
+    if (!f) return fail(CUPSSGB_ERR_INVALID, std::string("no field ") + (name ? name : ""));
+    const size_t n = (size_t)e->e->getSystemSizeX() * e->e->getSystemSizeY() * e->e->getSystemSizeZ();
+    for (size_t i = 0; i < n; ++i) host_real[i] = f->real_array[i].x;
+    return 0;
+  });
+}
+
+int cupssgb_write_field_csv(const char* path, const char* name, const float* values, int sx, int sy, int sz,
+                            int precision) {
+  NEED(path);
+  NEED(name);
+  NEED(values);
+  if (sx < 1 || sy < 1 || sz < 1 || precision < 0) return fail(CUPSSGB_ERR_INVALID, "bad sizes");
+  return guard([&] {
+    const int dim = (sy == 1 && sz == 1) ? 1 : (sz == 1 ? 2 : 3);
+    const std::string err = cupssgb_host::write_field_csv(path, name, values, sx, sy, sz, dim, precision);
+    return err.empty() ? 0 : fail(CUPSSGB_ERR_INVALID, err);
   });
 }
 

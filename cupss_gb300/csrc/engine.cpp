@@ -47,8 +47,15 @@ Solver::Solver(int sx, int sy, int sz, float dx, float dy, float dz, float dt)
 
 Solver::~Solver() {
   if (stream_) cudaStreamSynchronize(stream_);
-  for (cudaGraphExec_t& g : graph_)
-    if (g) cudaGraphExecDestroy(g);
+  if (out_stream_) cudaStreamSynchronize(out_stream_);
+  for (cudaEvent_t e : out_ready_)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : out_free_)
+    if (e) cudaEventDestroy(e);
+  if (out_stream_) cudaStreamDestroy(out_stream_);
+  for (auto& row : graph_)
+    for (cudaGraphExec_t& g : row)
+      if (g) cudaGraphExecDestroy(g);
   for (cudaEvent_t e : ev_pool_) cudaEventDestroy(e);
   for (void* p : allocs_) cudaFree(p);
   if (stream_) cudaStreamDestroy(stream_);
@@ -269,20 +276,20 @@ void Solver::prepare() {
       jit_kernel(turn_source(P, p, L, nl), "cupssgb_turn");
     }
   }
+  // A batch's launches follow its active span, which changes as members come and go, so
+  // its graphs are captured on first use; a single system's are final here.
+  if (!batch_) capture_all_graphs();
 }
 
 // Multiprocessors of the current device (152 on a GB300; also the answer without a GPU).
 static int sm_count() {
-  static int n = 0;
-  if (n > 0) return n;
   int dev = 0, v = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) !=
                                                 cudaSuccess || v <= 0) {
     cudaGetLastError();
     return 152;
   }
-  n = v;
-  return n;
+  return v;
 }
 
 bool Solver::turn_split() const {
@@ -386,7 +393,7 @@ void Solver::set_real(int f, const float* src, bool on_device, int m) {
   }
 }
 
-void Solver::to_real_scratch(int f, int m) {
+void Solver::to_real_scratch(int f, int m, float* dst) {
   const float2* st = state_[par_[f]][f] + (size_t)m * half_;
   const float2* spec = st;
   if (dim_ == 3) {
@@ -407,12 +414,39 @@ void Solver::to_real_scratch(int f, int m) {
   x.n_in = 1;
   x.in[0] = spec;
   x.n_prod = 1;
-  x.out[0] = scratch_real_;
+  x.out[0] = dst ? dst : scratch_real_;
   x.prod_n[0] = 1;
   x.prod_f[0][0] = 0;
   x.tw = tw_;
   check(launch_row_pass(x, stream_), "row pass (materialise)");
   ++launches_;
+}
+
+void Solver::snapshot_real(int f, float* host_dst, cudaEvent_t done) {
+  if (!prepared_) throw Error(kErrState, "snapshot before prepare");
+  if (f < 0 || f >= nfields()) throw Error(kErrInvalid, "bad field index");
+  if (!host_dst) throw Error(kErrInvalid, "null host buffer");
+  if (!out_stream_) {
+    check(cudaStreamCreateWithFlags(&out_stream_, cudaStreamNonBlocking), "output stream");
+    out_stage_.assign(nfields(), nullptr);
+    out_ready_.assign(nfields(), nullptr);
+    out_free_.assign(nfields(), nullptr);
+  }
+  if (!out_stage_[f]) {
+    out_stage_[f] = (float*)dalloc(npoints() * sizeof(float));
+    check(cudaEventCreateWithFlags(&out_ready_[f], cudaEventDisableTiming), "cudaEventCreate");
+    check(cudaEventCreateWithFlags(&out_free_[f], cudaEventDisableTiming), "cudaEventCreate");
+  } else {
+    // the previous copy of this field must have left the staging buffer
+    check(cudaStreamWaitEvent(stream_, out_free_[f], 0), "cudaStreamWaitEvent");
+  }
+  to_real_scratch(f, 0, out_stage_[f]);
+  check(cudaEventRecord(out_ready_[f], stream_), "cudaEventRecord");
+  check(cudaStreamWaitEvent(out_stream_, out_ready_[f], 0), "cudaStreamWaitEvent");
+  check(cudaMemcpyAsync(host_dst, out_stage_[f], npoints() * sizeof(float), cudaMemcpyDeviceToHost, out_stream_),
+        "snapshot copy");
+  check(cudaEventRecord(out_free_[f], out_stream_), "cudaEventRecord");
+  if (done) check(cudaEventRecord(done, out_stream_), "cudaEventRecord");
 }
 
 void Solver::get_real(int f, float* dst, bool on_device, int m) {
@@ -919,8 +953,10 @@ void Solver::step_once(uint32_t off, bool tick) {
 void Solver::advance(int nsteps) {
   if (!prepared_) throw Error(kErrState, "advance before prepare");
   if (batch_ && mvals_dirty_) upload_member_values();
-  if (!timing_)
-    for (; nsteps >= kGraphSteps; nsteps -= kGraphSteps) run_graph();
+  if (!timing_) {
+    for (int c = 0; c < 3; ++c)
+      for (; nsteps >= kGraphChunks[c]; nsteps -= kGraphChunks[c]) run_graph(c);
+  }
   for (int s = 0; s < nsteps; ++s) step_once(0, true);
 }
 

@@ -74,6 +74,14 @@ class Solver {
   void advance(int nsteps);
   void get_real(int f, float* dst, bool dst_on_device, int m = 0);
   void get_fourier(int f, float2* dst, bool dst_on_device, int m = 0);
+  // Output path of writeOut (src/field.cpp:350-402): copies the real values of field f
+  // into host memory without holding up later work on the solver's stream.  The field is
+  // materialised on the solver's stream into a device staging buffer of its own; the
+  // device-to-host copy then runs on a separate output stream, and `done` (if not null) is
+  // recorded there once the host copy is complete.  host_dst should be page-locked for the
+  // copy to be asynchronous.  A later snapshot of the same field first waits until the
+  // previous copy has left its staging buffer.
+  void snapshot_real(int f, float* host_dst, cudaEvent_t done);
 
   // ---- batches: n independent systems of this structure and grid in one solver ----
   // set_members(n) before prepare turns the solver into a batch.  Member 0 starts as the
@@ -81,7 +89,9 @@ class Solver {
   // then get its own prefactor values (same monomials), noise amplitude and seed.  Every
   // step launch covers all members (blockIdx.z = member); a member's noise counter is
   // its own step count, so its trajectory does not depend on the rest of the batch.
-  // Steps are replayed from CUDA graphs of kGraphSteps steps (single systems too).
+  // Steps are replayed from CUDA graphs of kGraphSteps, 4 and 1 steps (single systems
+  // too); a single system captures them at prepare, so advance() replays from its first
+  // call on.
   void set_members(int n);
   int members() const { return nmem_; }
   bool batched() const { return batch_; }
@@ -161,7 +171,8 @@ class Solver {
   // lkeep > 0: inverse-pass input positions with |n| >= lkeep along the line are zero
   void line_fwd_inv(int geo, int mode, const float2* in, float2* out, int xlimit, bool batch = false,
                     int lkeep = 0, bool pdl = false);
-  void to_real_scratch(int f, int m);
+  // real values of field f (member m) into dst (the real scratch array when null)
+  void to_real_scratch(int f, int m, float* dst = nullptr);
   void step_once(uint32_t off, bool tick);
   // batches
   void check_member(int m) const;
@@ -170,7 +181,10 @@ class Solver {
   void autotune();
   void zero_dynamic_buffers();
   void invalidate_graphs();
-  void run_graph();
+  // chunk index c: kGraphChunks[c] steps; parity: the ping-pong parity the graph starts at
+  void capture_graph(int c, int parity);
+  void capture_all_graphs();
+  void run_graph(int c);
   void row_pass_simple(int in_mode, const void* in, int out_mode, void* out, float scale);
   void forward_lines(float2* st);
   void channel_from_state(int f, float2* dst);
@@ -207,8 +221,9 @@ class Solver {
   float* mvals_d_[2] = {nullptr, nullptr};
   bool mvals_dirty_ = false;
   uint32_t step_off_ = 0;                        // step offset of the launches being issued
-  cudaGraphExec_t graph_[2] = {nullptr, nullptr};   // by parity of the step count
-  long long graph_launches_ = 0;                     // kernels per graph replay
+  static constexpr int kGraphChunks[3] = {kGraphSteps, 4, 1};
+  cudaGraphExec_t graph_[3][2] = {};   // by chunk and by the ping-pong parity it starts at
+  long long graph_launches_[3] = {};   // kernels per replay of each chunk
 
   cudaStream_t stream_ = nullptr;
   float2* tw_ = nullptr;
@@ -219,6 +234,11 @@ class Solver {
   float* scratch_real_ = nullptr;
   float2* scratch_spec_ = nullptr;
   float2* scratch_full_ = nullptr;   // reference-layout full spectrum, allocated on first use
+  // output path (snapshot_real), created on first use
+  cudaStream_t out_stream_ = nullptr;
+  std::vector<float*> out_stage_;          // per field: staging copy of the real values
+  std::vector<cudaEvent_t> out_ready_;     // per field: staging copy written (solver stream)
+  std::vector<cudaEvent_t> out_free_;      // per field: staging copy read out (output stream)
   std::vector<void*> allocs_;
   Phase phases_[2];              // 0: non-dynamic, 1: dynamic
   // kernel timing

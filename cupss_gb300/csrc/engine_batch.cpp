@@ -294,45 +294,68 @@ std::string Solver::tune_report() const {
 }
 
 void Solver::invalidate_graphs() {
-  for (cudaGraphExec_t& g : graph_)
-    if (g) {
-      cudaGraphExecDestroy(g);
-      g = nullptr;
-    }
+  for (auto& row : graph_)
+    for (cudaGraphExec_t& g : row)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
 }
 
-// Replays kGraphSteps steps from the graph for the current ping-pong parity (every
-// field flips once per step, so an even number of steps returns to it).
-void Solver::run_graph() {
-  static_assert(kGraphSteps % 2 == 0, "graphs must span an even number of steps");
-  const int key = par_.empty() ? 0 : par_[0];
-  if (!graph_[key]) {
-    const long long s0 = step_, l0 = launches_;
-    cudaGraph_t g = nullptr;
-    check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
-    try {
-      // the launches of step s use step count + s; one counter update ends the graph
-      for (int s = 0; s < kGraphSteps; ++s) step_once((uint32_t)s, s == kGraphSteps - 1);
-    } catch (...) {
-      cudaStreamEndCapture(stream_, &g);
-      if (g) cudaGraphDestroy(g);
-      step_ = s0;
-      launches_ = l0;
-      throw;
-    }
-    check(cudaStreamEndCapture(stream_, &g), "cudaStreamEndCapture");
-    cudaGraphExec_t ex = nullptr;
-    const cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
-    cudaGraphDestroy(g);
-    check(e, "cudaGraphInstantiate");
-    graph_[key] = ex;
-    graph_launches_ = launches_ - l0;
+// Records kGraphChunks[c] steps starting at ping-pong parity `parity` into a graph and
+// instantiates it.  Nothing runs: the step count, launch count and parities are restored
+// afterwards, and run_graph applies the chunk's effect on them when it replays it.
+void Solver::capture_graph(int c, int parity) {
+  const int n = kGraphChunks[c];
+  const long long s0 = step_, l0 = launches_;
+  const std::vector<int> par0 = par_;
+  std::fill(par_.begin(), par_.end(), parity);
+  cudaGraph_t g = nullptr;
+  auto restore = [&] {
     step_ = s0;
     launches_ = l0;
+    par_ = par0;
+  };
+  check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+  try {
+    // the launches of step s use step count + s; one counter update ends the graph
+    for (int s = 0; s < n; ++s) step_once((uint32_t)s, s == n - 1);
+  } catch (...) {
+    cudaStreamEndCapture(stream_, &g);
+    if (g) cudaGraphDestroy(g);
+    restore();
+    throw;
   }
-  check(cudaGraphLaunch(graph_[key], stream_), "cudaGraphLaunch");
-  launches_ += graph_launches_;
-  step_ += kGraphSteps;
+  const long long nl = launches_ - l0;
+  restore();
+  check(cudaStreamEndCapture(stream_, &g), "cudaStreamEndCapture");
+  cudaGraphExec_t ex = nullptr;
+  const cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+  cudaGraphDestroy(g);
+  check(e, "cudaGraphInstantiate");
+  // the graph's work is uploaded to the device now, not at its first replay
+  check(cudaGraphUpload(ex, stream_), "cudaGraphUpload");
+  graph_[c][parity] = ex;
+  graph_launches_[c] = nl;
+}
+
+void Solver::capture_all_graphs() {
+  for (int c = 0; c < 3; ++c)
+    for (int parity = 0; parity < 2; ++parity)
+      if (!graph_[c][parity]) capture_graph(c, parity);
+  check(cudaStreamSynchronize(stream_), "graph upload");
+}
+
+// Replays chunk c from the graph for the current ping-pong parity (every field flips
+// once per step, so all fields share one parity).
+void Solver::run_graph(int c) {
+  const int key = par_.empty() ? 0 : par_[0];
+  if (!graph_[c][key]) capture_graph(c, key);
+  check(cudaGraphLaunch(graph_[c][key], stream_), "cudaGraphLaunch");
+  launches_ += graph_launches_[c];
+  step_ += kGraphChunks[c];
+  if (kGraphChunks[c] & 1)
+    for (int& p : par_) p ^= 1;
 }
 
 }  // namespace cupssgb

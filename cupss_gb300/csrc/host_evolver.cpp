@@ -57,6 +57,7 @@ void evolver::common_constructor() {
   throw_errors_ = false;
   seed_set_ = false;
   seed_ = 0;
+  writer_ = nullptr;
   if (sz == 1 && sy == 1) {
     dimension = 1;
     blocks = 1;
@@ -73,6 +74,16 @@ void evolver::common_constructor() {
 }
 
 evolver::~evolver() {
+  if (writer_) {
+    // every queued file is written before the device state goes away
+    const std::string err = writer_->flush();
+    delete writer_;
+    writer_ = nullptr;
+    if (!err.empty()) {
+      std::cout << err << std::endl;
+      if (!throw_errors_) std::exit(1);
+    }
+  }
   for (field* f : fields) delete f;
   delete _parser;
   if (solver_) cupssgb_solver_destroy(solver_);
@@ -110,8 +121,9 @@ void evolver::setNoiseSeed(unsigned long long seed) {
 }
 
 int evolver::createFromFile(const std::string& file) {
-  CUPSS_GUARD(_parser->createFromFile(file));
-  return 0;
+  int r = 0;
+  CUPSS_GUARD(r = _parser->createFromFile(file));
+  return r;
 }
 
 bool evolver::has_callbacks() const {
@@ -362,6 +374,7 @@ int evolver::advanceTime() {
     if (throw_errors_) throw std::runtime_error("advanceTime before prepareProblem");
     fatal("ERROR: advanceTime before prepareProblem");
   }
+  report_output_error();
   if (currentTimeStep % writeEveryNSteps == 0) writeOut();
   if (has_callbacks()) {
     run_callbacks_step();
@@ -409,8 +422,57 @@ int evolver::advanceTimeSteps(int n) {
   return 0;
 }
 
+// GPU fields are copied out on the engine's output stream and written by the background
+// writer, so the steps queued after this call run while the files are formatted; RUN_CPU
+// fields (host arrays refreshed every step) are written here.  Same files, format and
+// NaN rule as the reference (src/evolver.cpp:228-232, src/field.cpp:350-402).
 void evolver::writeOut() {
-  for (field* f : fields) f->writeToFile(currentTimeStep, dimension, writePrecision);
+  report_output_error();
+  const size_t n = (size_t)sx * sy * sz;
+  for (size_t i = 0; i < fields.size(); ++i) {
+    field* f = fields[i];
+    if (!f->outputToFile) continue;
+    if (!with_cuda || !solver_) {
+      f->writeToFile(currentTimeStep, dimension, writePrecision);
+      continue;
+    }
+    if (!writer_) {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      writer_ = new cupssgb_host::OutputWriter(dev, n);
+    }
+    float* buf = nullptr;
+    void* done = nullptr;
+    int rc = writer_->acquire(&buf, &done);
+    if (rc == 0) {
+      rc = cupssgb_solver_snapshot_real(solver_, (int)i, buf, done);
+      if (rc == 0)
+        writer_->submit("data/" + f->name + ".csv." + std::to_string(currentTimeStep), f->name, sx, sy, sz,
+                        dimension, writePrecision, buf, done);
+      else
+        writer_->release(buf, done);
+    }
+    if (rc != 0) {
+      if (throw_errors_) throw std::runtime_error(cupssgb_last_error());
+      fatal(std::string("ERROR: output of field ") + f->name + ": " + cupssgb_last_error());
+    }
+  }
+}
+
+void evolver::report_output_error() {
+  if (!writer_) return;
+  const std::string err = writer_->error();
+  if (err.empty()) return;
+  if (throw_errors_) throw std::runtime_error(err);
+  fatal(err);
+}
+
+void evolver::flushOutput() {
+  if (!writer_) return;
+  const std::string err = writer_->flush();
+  if (err.empty()) return;
+  if (throw_errors_) throw std::runtime_error(err);
+  fatal(err);
 }
 
 void evolver::setVerbose() { verbose = true; }

@@ -6,28 +6,33 @@
 #include <ctime>
 #include <fstream>
 #include <iostream>
+#include <stdexcept>
 #include <string>
 
 #include "../../include/cupss.h"
 
 namespace {
-void require_field(evolver* e, const std::string& name, const char* what) {
-  if (e->existsField(name) < 0) {
-    std::cout << "ERROR in " << what << ", " << name << " not found" << std::endl;
-    std::exit(1);
-  }
+// The reference prints the message and exits with status 1; an evolver driven through
+// the C-ABI (setThrowOnError) throws instead.
+[[noreturn]] void init_error(bool throw_errors, const std::string& msg) {
+  if (throw_errors) throw std::runtime_error(msg);
+  std::cout << msg << std::endl;
+  std::exit(1);
+}
+void require_field(evolver* e, bool throw_errors, const std::string& name, const char* what) {
+  if (e->existsField(name) < 0) init_error(throw_errors, std::string("ERROR in ") + what + ", " + name + " not found");
 }
 }  // namespace
 
 void evolver::initializeUniform(std::string f, float value) {
-  require_field(this, f, "initialize uniform");
+  require_field(this, throw_errors_, f, "initialize uniform");
   float2* a = fieldsMap[f]->real_array;
   const size_t n = (size_t)sx * sy * sz;
   for (size_t i = 0; i < n; ++i) a[i].x = value;
 }
 
 void evolver::initializeUniformNoise(std::string f, float value) {
-  require_field(this, f, "initialize uniform");
+  require_field(this, throw_errors_, f, "initialize uniform");
   std::srand(time(0));
   float2* a = fieldsMap[f]->real_array;
   const size_t n = (size_t)sx * sy * sz;
@@ -35,7 +40,7 @@ void evolver::initializeUniformNoise(std::string f, float value) {
 }
 
 void evolver::initializeNormalNoise(std::string f, float mean, float sigma) {
-  require_field(this, f, "initialize uniform");
+  require_field(this, throw_errors_, f, "initialize uniform");
   std::srand(time(0));
   float2* a = fieldsMap[f]->real_array;
   const size_t n = (size_t)sx * sy * sz;
@@ -49,14 +54,12 @@ void evolver::initializeNormalNoise(std::string f, float mean, float sigma) {
 }
 
 void evolver::initializeHalfSystem(std::string f, float val1, float val2, float xi, int direction) {
-  require_field(this, f, "initialize half system");
+  require_field(this, throw_errors_, f, "initialize half system");
   if (xi <= 0.0) {
-    std::cout << "ERROR in initialize, interface width cannot be 0 or negative" << std::endl;
-    std::exit(1);
+    init_error(throw_errors_, "ERROR in initialize, interface width cannot be 0 or negative");
   }
   if (direction < 1 || direction > 3) {
-    std::cout << "ERROR in initialize, direction can be 1, 2 or 3 for x, y, z, respectively" << std::endl;
-    std::exit(1);
+    init_error(throw_errors_, "ERROR in initialize, direction can be 1, 2 or 3 for x, y, z, respectively");
   }
   std::srand(time(0));
   const int rev = direction == 1 ? sx : (direction == 2 ? sy : sz);
@@ -72,11 +75,9 @@ void evolver::initializeHalfSystem(std::string f, float val1, float val2, float 
 
 void evolver::initializeDroplet(std::string f, float val1, float val2, float radius, float xi, int p_x,
                                 int p_y, int p_z) {
-  require_field(this, f, "initialize droplet");
+  require_field(this, throw_errors_, f, "initialize droplet");
   if (xi <= 0.0 || radius <= 0.0) {
-    std::cout << "ERROR in initialize, droplet radius and interface width cannot be 0 or negative"
-              << std::endl;
-    std::exit(1);
+    init_error(throw_errors_, "ERROR in initialize, droplet radius and interface width cannot be 0 or negative");
   }
   const int x0 = p_x % sx, y0 = p_y % sy, z0 = p_z % sz;
   std::srand(time(0));
@@ -92,11 +93,9 @@ void evolver::initializeDroplet(std::string f, float val1, float val2, float rad
 }
 
 void evolver::addDroplet(std::string f, float val, float radius, float xi, int p_x, int p_y, int p_z) {
-  require_field(this, f, "initialize droplet");
+  require_field(this, throw_errors_, f, "initialize droplet");
   if (xi <= 0.0 || radius <= 0.0) {
-    std::cout << "ERROR in initialize, droplet radius and interface width cannot be 0 or negative"
-              << std::endl;
-    std::exit(1);
+    init_error(throw_errors_, "ERROR in initialize, droplet radius and interface width cannot be 0 or negative");
   }
   const int x0 = p_x % sx, y0 = p_y % sy, z0 = p_z % sz;
   std::srand(time(0));
@@ -112,11 +111,10 @@ void evolver::addDroplet(std::string f, float val, float radius, float xi, int p
 }
 
 void evolver::initializeFromFile(std::string f, std::string file, int skiprows, char delimiter) {
-  require_field(this, f, "initialize droplet");
+  require_field(this, throw_errors_, f, "initialize droplet");
   FILE* chk = std::fopen(file.c_str(), "r");
   if (chk == nullptr) {
-    std::cout << "Initial file: " << file << " not found. Doing nothing" << std::endl;
-    std::exit(1);
+    init_error(throw_errors_, "Initial file: " + file + " not found. Doing nothing");
   }
   std::fclose(chk);
   std::ifstream in(file.c_str());
@@ -126,9 +124,8 @@ void evolver::initializeFromFile(std::string f, std::string file, int skiprows, 
   float2* a = fieldsMap[f]->real_array;
   for (size_t i = 0; i < n; ++i) {
     if (!std::getline(in, posx, delimiter)) {
-      std::cout << "Incompatible number of lines on file " << file << ", only " << i + 1
-                << " found for a system size of " << n << std::endl;
-      std::exit(1);
+      init_error(throw_errors_, "Incompatible number of lines on file " + file + ", only " + std::to_string(i + 1) +
+                                    " found for a system size of " + std::to_string(n));
     }
     if (dimension > 1) std::getline(in, posy, delimiter);
     if (dimension > 2) std::getline(in, posz, delimiter);

@@ -1,35 +1,31 @@
-// CUDA status helpers (reference behaviour: src/cu_utils.cpp:4-37).
+// check_error / check_device of the drop-in API (inc/cupss/cu_utils.h:6-7 in the
+// reference).  Both keep the reference's contract -- a failed CUDA status or a machine
+// without a GPU ends the program with status 1 -- on top of this library's status-code
+// query cupssgb_device_info.
+#include <cstdio>
 #include <cstdlib>
-#include <iostream>
+#include <string>
+#include <vector>
 
 #include "../../include/cupss.h"
+#include "../../include/cupss_gb300.h"
 
 void check_error(cudaError_t err) {
-  if (err != cudaSuccess) {
-    std::cerr << "CUDA Runtime Error" << std::endl;
-    std::cerr << cudaGetErrorString(err) << std::endl;
-    std::exit(1);
-  }
+  if (err == cudaSuccess) return;
+  std::fprintf(stderr, "cupss: CUDA call failed (%s): %s\n", cudaGetErrorName(err), cudaGetErrorString(err));
+  std::exit(1);
 }
 
 void check_device() {
-  int n = 0, rt = 0, drv = 0;
-  check_error(cudaGetDeviceCount(&n));
-  check_error(cudaRuntimeGetVersion(&rt));
-  check_error(cudaDriverGetVersion(&drv));
-  if (n == 0) {
-    std::cerr << "No CUDA devices found but trying to run on CUDA, exiting." << std::endl;
+  std::vector<char> text(4096);
+  const int n = cupssgb_device_info(text.data(), (int)text.size());
+  if (n < 0) {
+    std::fprintf(stderr, "cupss: device query failed: %s\n", cupssgb_last_error());
     std::exit(1);
   }
-  std::cout << "Devices found:" << std::endl;
-  for (int i = 0; i < n; ++i) {
-    cudaDeviceProp prop;
-    cudaGetDeviceProperties(&prop, i);
-    std::cout << "Device " << i << ": " << prop.name << std::endl;
+  if (n == 0) {
+    std::fprintf(stderr, "cupss: a GPU run was asked for but no CUDA device is visible\n");
+    std::exit(1);
   }
-  std::cout << "CUDA Driver Version: " << drv / 1000 << "." << (drv % 100) / 10 << std::endl;
-  std::cout << "CUDA Runtime Version: " << rt / 1000 << "." << (rt % 100) / 10 << std::endl;
-  if (rt > drv)
-    std::cout << "WARNING: runtime version is not supported by driver. Solver might not work properly"
-              << std::endl;
+  std::printf("cupss: %d CUDA device%s\n%s", n, n == 1 ? "" : "s", text.data());
 }

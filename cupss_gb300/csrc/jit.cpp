@@ -6,7 +6,8 @@
 // (numerical prefactor values stay in the kernel parameter block, so updateParameter
 // needs no recompilation), compiles it for the running GPU with NVRTC and launches the
 // cubin through the runtime's library API.  Compiled kernels are cached per process by
-// source text.
+// device and source text: each device gets a build for its own architecture, with the
+// shared-memory limit raised on that device.
 #include "jit.h"
 
 #include <nvrtc.h>
@@ -33,7 +34,7 @@ namespace {
 const char* const kJitFastOpts[] = {"--prec-div=false", "--prec-sqrt=false"};
 
 std::mutex g_mu;
-std::map<std::string, cudaKernel_t> g_cache;
+std::map<std::pair<int, std::string>, cudaKernel_t> g_cache;   // (device, source) -> kernel
 
 std::string pow_expr(const char* base, int n) {
   if (n <= 0) return "";
@@ -177,12 +178,14 @@ std::string jit_generate_turn(const LineParams& p, int L, int NL, int warps, boo
 
 cudaKernel_t jit_kernel(const std::string& source, const char* entry) {
   std::lock_guard<std::mutex> lk(g_mu);
-  auto it = g_cache.find(source);
-  if (it != g_cache.end()) return it->second;
   int dev = 0, major = 0, minor = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
-  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) throw Error(kErrCuda, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+  auto it = g_cache.find({dev, source});
+  if (it != g_cache.end()) return it->second;
+  if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev) != cudaSuccess)
+    throw Error(kErrCuda, "compute capability query failed");
   // sm_103a on GB300; other Blackwell parts get their own arch-specific target
   const std::string arch = "--gpu-architecture=sm_" + std::to_string(major * 10 + minor) + "a";
   nvrtcProgram prog;
@@ -205,14 +208,14 @@ cudaKernel_t jit_kernel(const std::string& source, const char* entry) {
   nvrtcGetCUBIN(prog, cubin.data());
   nvrtcDestroyProgram(&prog);
   cudaLibrary_t lib;
-  cudaError_t e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+  e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
   if (e != cudaSuccess) throw Error(kErrCuda, std::string("cudaLibraryLoadData: ") + cudaGetErrorString(e));
   cudaKernel_t k;
   e = cudaLibraryGetKernel(&k, lib, entry);
   if (e != cudaSuccess) throw Error(kErrCuda, std::string("cudaLibraryGetKernel: ") + cudaGetErrorString(e));
   e = cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
   if (e != cudaSuccess) throw Error(kErrCuda, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
-  g_cache[source] = k;
+  g_cache[{dev, source}] = k;
   return k;
 }
 

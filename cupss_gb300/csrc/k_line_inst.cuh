@@ -6,11 +6,8 @@
 
 namespace cupssgb {
 template <class K>
-static cudaError_t set_smem_attr(K kernel, bool& done) {
-  if (done) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-  if (e == cudaSuccess) done = true;
-  return e;
+static cudaError_t set_smem_attr(K kernel, std::atomic<unsigned long long>& done) {
+  return raise_smem_limit((const void*)kernel, done);
 }
 }  // namespace cupssgb
 
@@ -18,7 +15,7 @@ static cudaError_t set_smem_attr(K kernel, bool& done) {
   namespace cupssgb {                                                                           \
   cudaError_t launch_line_##L(const LineParams& p, int nl, size_t smem, dim3 grid,              \
                               cudaStream_t st, bool pdl) {                                      \
-    static bool a0 = false, a1 = false, a2 = false;                                             \
+    static std::atomic<unsigned long long> a0{0}, a1{0}, a2{0}; /* devices with the smem limit */ \
     LaunchCfg lc(grid, dim3(p.W, LineCfg<L>::M, nl), smem, st, pdl);                            \
     cudaError_t e = cudaSuccess;                                                                \
     if (p.mode != kModeTurn) {                                                                  \

@@ -13,17 +13,13 @@ static bool row_is_one(const XParams& p) {
 template <int LX, bool SP>
 static cudaError_t launch_row_form(const XParams& p, cudaStream_t st, int nz, bool pdl) {
   using C = RowCfg<LX, SP>;
-  static bool attr = false, attr_one = false;
+  static std::atomic<unsigned long long> attr{0}, attr_one{0};   // devices with the smem limit raised
   dim3 block(C::M, C::RW);
   dim3 grid((p.rows + C::RW - 1) / C::RW, 1, nz);
   if (row_is_one(p)) {
     const size_t smem = 2 * (size_t)C::RW * C::PL * sizeof(float2);   // two transpose buffers
-    if (!attr_one) {
-      cudaError_t e = cudaFuncSetAttribute(row_pass_one<LX, SP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           220 * 1024);
-      if (e != cudaSuccess) return e;
-      attr_one = true;
-    }
+    const cudaError_t e = raise_smem_limit((const void*)row_pass_one<LX, SP>, attr_one);
+    if (e != cudaSuccess) return e;
     LaunchCfg lc(grid, block, smem, st, pdl);
     return cudaLaunchKernelEx(&lc.cfg, row_pass_one<LX, SP>, p);
   }
@@ -34,11 +30,8 @@ static cudaError_t launch_row_form(const XParams& p, cudaStream_t st, int nz, bo
   } else {
     kern = row_pass<LX>;
   }
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  const cudaError_t e = raise_smem_limit((const void*)kern, attr);
+  if (e != cudaSuccess) return e;
   LaunchCfg lc(grid, block, smem, st, pdl);
   return cudaLaunchKernelEx(&lc.cfg, kern, p);
 }

@@ -1,9 +1,27 @@
 // Host-side launchers for the engine kernels (implemented in k_*.cu).
 #pragma once
 #include <cuda_runtime.h>
+
+#include <atomic>
+
 #include "engine_types.h"
 
 namespace cupssgb {
+
+// Raises a kernel's dynamic shared-memory limit to 220 KiB on the current device.  The
+// attribute belongs to one device, so `done` records, one bit per device ordinal, the
+// devices where it is set; the bit is set after a successful call, and two threads that
+// race both make the (idempotent) call.
+inline cudaError_t raise_smem_limit(const void* kernel, std::atomic<unsigned long long>& done) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
+  if (bit && (done.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+  if (e == cudaSuccess && bit) done.fetch_or(bit, std::memory_order_acq_rel);
+  return e;
+}
 
 // Launch configuration; pdl: programmatic stream serialization, so the kernel may
 // become resident while its predecessor in the stream drains (the step kernels wait

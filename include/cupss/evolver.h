@@ -14,6 +14,9 @@ class field;
 class parser;
 struct pres;
 struct cupssgb_solver;
+namespace cupssgb_host {
+class OutputWriter;
+}
 
 class evolver {
  private:
@@ -34,6 +37,8 @@ class evolver {
   void sync_host_arrays();
   void run_callbacks_step();
   bool has_callbacks() const;
+  cupssgb_host::OutputWriter* writer_;   // writes writeOut's files in the background
+  void report_output_error();
 
  public:
   int dimension;
@@ -110,6 +115,11 @@ class evolver {
   int advanceTimeSteps(int n);
   // Parse/state errors throw std::runtime_error instead of printing and exiting.
   void setThrowOnError(bool on);
+  // writeOut queues its files; a background thread writes them while the steps go on.
+  // Waits until every queued file is written (the destructor does too).  A file that
+  // could not be written, or a NaN in a field, is reported here or at the next writeOut
+  // or advanceTime, the reference's way (message, exit status 1) unless errors throw.
+  void flushOutput();
   cupssgb_solver* solverHandle();
 };
 

@@ -123,6 +123,15 @@ int cupssgb_solver_set_real_pairs_device(cupssgb_solver* s, int field, const flo
                                          const float* dev_dealiased_pairs);
 /* Waits for all work queued on the solver's stream. */
 int cupssgb_solver_synchronize(cupssgb_solver* s);
+/* Output path of writeOut (src/field.cpp:350-402): copies the real values of a field into
+ * host memory without stalling the step.  The field is materialised on the solver's
+ * stream into a staging buffer of its own (allocated on the first call for that field);
+ * the device-to-host copy runs on a separate output stream, so steps queued after this
+ * call overlap with it.  done_event (a cudaEvent_t, may be NULL) is recorded on the
+ * output stream once host_real holds the values; host_real should be page-locked
+ * (cupssgb_host_alloc) for the copy to be asynchronous.  A later snapshot of the same
+ * field waits until the previous copy has left the staging buffer. */
+int cupssgb_solver_snapshot_real(cupssgb_solver* s, int field, float* host_real, void* done_event);
 /* Steps taken so far, kernels launched so far, device bytes held. */
 long long cupssgb_solver_step_count(const cupssgb_solver* s);
 long long cupssgb_solver_launch_count(const cupssgb_solver* s);
@@ -190,6 +199,12 @@ int cupssgb_host_alloc(long long bytes, void** out);
 int cupssgb_host_free(void* p);
 /* Selects the CUDA device of the calling thread for subsequently created solvers. */
 int cupssgb_set_device(int device);
+/* Visible CUDA devices: returns their number (0 when there is none) or a negative
+ * status, and writes one line per device ("<index>: <name>, <SMs> SMs, sm_<cc>, <MiB> MiB")
+ * followed by a "driver <v>, runtime <v>" line into buf (the return value does not count
+ * the text; buf may be NULL).  Backs check_device of the drop-in API
+ * (inc/cupss/cu_utils.h:7 in the reference). */
+int cupssgb_device_info(char* buf, int buflen);
 
 /* Forward transform of one real field without any device allocation.  No counterpart
  * in the reference: it exists for callers that must not let a library allocate
@@ -238,6 +253,38 @@ int cupssgb_evolver_prepare(cupssgb_evolver* e);
 int cupssgb_evolver_advance(cupssgb_evolver* e, int nsteps);
 /* evolver::writeOut (src/evolver.cpp:228-232). */
 int cupssgb_evolver_write_out(cupssgb_evolver* e);
+/* Waits until every field file queued by writeOut is written (files are written by a
+ * background thread while the steps go on).  Returns 0, or CUPSSGB_ERR_INVALID with
+ * the first failure (e.g. "NaN found in field phi") in cupssgb_last_error(). */
+int cupssgb_evolver_flush_output(cupssgb_evolver* e);
+/* Builds the system from a system file (evolver::createFromFile, src/parser.cpp:11-96):
+ * sections "Fields" (name dynamic output), "Parameters" (name value) and "Equations". */
+int cupssgb_evolver_create_from_file(cupssgb_evolver* e, const char* path);
+/* Initial conditions written into the host array of a field (fieldsReal), before
+ * prepareProblem (src/initializers.cpp:14-267; same formulas, the noise ones draw from
+ * the C library's rand() seeded with time(NULL) like the reference). */
+int cupssgb_evolver_initialize_uniform(cupssgb_evolver* e, const char* field, float value);
+int cupssgb_evolver_initialize_uniform_noise(cupssgb_evolver* e, const char* field, float amplitude);
+int cupssgb_evolver_initialize_normal_noise(cupssgb_evolver* e, const char* field, float mean, float sigma);
+int cupssgb_evolver_initialize_half_system(cupssgb_evolver* e, const char* field, float value1, float value2,
+                                           float interface_width, int direction);
+int cupssgb_evolver_initialize_droplet(cupssgb_evolver* e, const char* field, float value_out, float value_in,
+                                       float radius, float interface_width, int center_x, int center_y,
+                                       int center_z);
+int cupssgb_evolver_add_droplet(cupssgb_evolver* e, const char* field, float value, float radius,
+                                float interface_width, int center_x, int center_y, int center_z);
+int cupssgb_evolver_initialize_from_file(cupssgb_evolver* e, const char* field, const char* path, int skiprows,
+                                         char delimiter);
+/* Copies the host array of a field (fieldsReal[field][i].x) into host_real; no device
+ * access (after prepareProblem it holds what the host wrote, not the evolved field). */
+int cupssgb_evolver_get_host_real(cupssgb_evolver* e, const char* field, float* host_real);
+/* Writes values (sx*sy*sz floats) as one field file in the reference's CSV format to
+ * path: header "x, [y, [z, ]]<name>", one "i, [j, [k, ]]value" line per point with
+ * `precision` decimals (src/field.cpp:350-402).  The dimension follows the reference's
+ * rule (sy = sz = 1: 1D; sz = 1: 2D).  A NaN value stops the file with
+ * CUPSSGB_ERR_INVALID ("NaN found in field <name>"). */
+int cupssgb_write_field_csv(const char* path, const char* name, const float* values, int sx, int sy, int sz,
+                            int precision);
 /* copyAllDataToHost then field.real_array[.].x / comp_array for one field. */
 int cupssgb_evolver_get_real(cupssgb_evolver* e, const char* field, float* host_real);
 int cupssgb_evolver_get_fourier(cupssgb_evolver* e, const char* field, float* host_complex);

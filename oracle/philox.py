@@ -29,6 +29,9 @@ realisation the GPU used:
 """
 from __future__ import annotations
 
+import ctypes
+import threading
+
 import numpy as np
 
 M0 = np.uint64(0xD2511F53)
@@ -68,8 +71,41 @@ def normal_pair(x0, x1, dtype=np.float64):
     return r * np.cos(ang), r * np.sin(ang)
 
 
+_C_LIB = None
+_C_LOCK = threading.Lock()
+
+
+def _c_lib():
+    """The C restatement (oracle/noise.c), built on first use; None without a C compiler."""
+    global _C_LIB
+    with _C_LOCK:
+        if _C_LIB is None:
+            try:
+                from . import build
+                lib = ctypes.CDLL(build.build())
+                lib.oracle_fourier_noise.restype = None
+                lib.oracle_fourier_noise.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong,
+                                                     ctypes.c_uint, ctypes.c_uint, ctypes.c_void_p]
+                _C_LIB = lib
+            except Exception:
+                _C_LIB = False
+        return _C_LIB or None
+
+
 def fourier_noise(sx, sy, sz, seed, step, field_id, dtype=np.complex128):
-    """Full (reference-layout, [kz][ky][kx]) Hermitian noise field for one step."""
+    """Full (reference-layout, [kz][ky][kx]) Hermitian noise field for one step, from the C
+    restatement when it builds, else from the numpy one below (same values)."""
+    lib = _c_lib()
+    if lib is None:
+        return fourier_noise_numpy(sx, sy, sz, seed, step, field_id, dtype)
+    out = np.empty((sz, sy, sx), np.complex128)
+    lib.oracle_fourier_noise(sx, sy, sz, int(seed) & 0xFFFFFFFFFFFFFFFF, int(step) & 0xFFFFFFFF,
+                             int(field_id) & 0xFFFFFFFF, out.ctypes.data)
+    return out.astype(dtype, copy=False)
+
+
+def fourier_noise_numpy(sx, sy, sz, seed, step, field_id, dtype=np.complex128):
+    """Full (reference-layout, [kz][ky][kx]) Hermitian noise field for one step (numpy)."""
     N = sx * sy * sz
     k0 = np.uint32(seed & 0xFFFFFFFF)
     k1 = np.uint32((seed >> 32) & 0xFFFFFFFF)

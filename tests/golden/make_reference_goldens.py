@@ -29,7 +29,9 @@ def load(path, dims):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_reference_goldens.py <path of a cuPSS checkout>")
+    root = sys.argv[1]
     bt = os.path.join(root, "tests", "base_truths")
     out = {}
     for name in sorted(os.listdir(bt)):

@@ -1,0 +1,164 @@
+"""Parity at the benchmark configurations' own sizes (GPU engine vs the FP64 oracle).
+
+The oracle (oracle/ref_solver.py) restates the reference GPU step op for op with full
+complex FFTs in float64 and is fed the engine's own Fourier-space noise realisation
+(oracle/philox.py, C restatement oracle/noise.c), so every run below compares one
+trajectory with the same trajectory, noise included.  Relative L2 over the whole field;
+each test prints the measured value and states its bound:
+
+* 3D Cahn-Hilliard + conserved noise at 256^3 (the benchmark workload), 50 steps;
+* the same system at 128^3 for 1000 steps: the relative L2 <= 1e-5 bar after 1000
+  steps;
+* 2D model H at 1024^2 (six fields, lagged Stokes velocity), 200 steps, every field;
+* 2D Cahn-Hilliard at 256^2 for the whole 10,000-step run.  Spinodal decomposition
+  amplifies every rounding difference (linear growth rate up to 1/4 per unit time, and
+  the run reaches t = 100), so two FP32 codes with different FFT roundings -- this one
+  and the reference's cuFFT -- part too.  The test states that drift against the FP64
+  oracle and checks what survives it: the conserved mean, the radial structure factor
+  and the field's distribution.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle.philox import NoiseProvider
+from oracle.ref_parser import System
+from oracle.ref_solver import RefSolver
+
+pytestmark = pytest.mark.gpu
+
+WORKERS = os.cpu_count() or 1
+
+
+@pytest.fixture(autouse=True)
+def _in_tmp(tmp_path, monkeypatch, built_lib):
+    monkeypatch.chdir(tmp_path)
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64).ravel()
+    b = np.asarray(b, np.float64).ravel()
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def init_field(n, lo, hi):
+    from cupss_gb300.workloads import splitmix64_uniform
+    return splitmix64_uniform(n, 20261203, lo, hi)
+
+
+def build_pair(shape, dt, fields, params, eqs, noises, init, seed=42):
+    import cupss_gb300 as c
+    sx, sy, sz = shape
+    s = System()
+    e = c.Evolver(True, sx, sy, sz, dt=dt, write_every=10 ** 9)
+    for n, dyn in fields:
+        s.create_field(n, dyn)
+        e.createField(n, dyn)
+    for k, v in params.items():
+        s.add_parameter(k, v)
+        e.addParameter(k, v)
+    for q in eqs:
+        s.add_equation(q)
+        e.addEquation(q)
+    for f, a in noises:
+        s.add_noise(f, a)
+        e.addNoise(f, a)
+    e.setNoiseSeed(seed)
+    r = RefSolver(s, sx, sy, sz, dt=dt, precision="f64", noise=NoiseProvider(sx, sy, sz, seed),
+                  fft_workers=WORKERS)
+    for n, arr in init.items():
+        r.set_real(n, arr)
+        e.setReal(n, arr)
+    r.prepare()
+    e.prepareProblem()
+    return e, r
+
+
+CH_EQ = "dt phi + q^2*(a + k*q^2)*phi = -b*q^2*phi^3"
+
+
+def ch3d(n, steps):
+    init = {"phi": init_field(n ** 3, -0.05, 0.05)}
+    e, r = build_pair((n, n, n), 0.005, [("phi", True)], {"a": -1.0, "b": 1.0, "k": 1.0, "T": 0.01}, [CH_EQ],
+                      [("phi", "2*T*q^2")], init)
+    e.advanceTime(steps)
+    r.advance(steps)
+    err = rel_l2(e.getReal("phi"), r.real_field("phi"))
+    e.close()
+    return err
+
+
+def test_ch3d_256_conserved_noise_full_size():
+    # the benchmark workload itself: 256^3, dt = 0.005, T = 0.01, 50 steps
+    err = ch3d(256, 50)
+    print("3D CH 256^3 + noise, 50 steps: rel L2 %.3e" % err)
+    assert err < 1e-5
+
+
+def test_ch3d_128_conserved_noise_1000_steps():
+    err = ch3d(128, 1000)
+    print("3D CH 128^3 + noise, 1000 steps: rel L2 %.3e" % err)
+    assert err < 1e-5
+
+
+MODEL_H = dict(
+    fields=[("phi", True), ("iqxphi", False), ("iqyphi", False), ("lapphi", False), ("vx", False), ("vy", False)],
+    params={"a": -1.0, "b": 1.0, "k": 4.0, "eta": 1.0, "T": 0.001},
+    eqs=["dt phi + q^2*(a + k*q^2)*phi = -b*q^2*phi^3 - vx*iqxphi - vy*iqyphi",
+         "iqxphi = iqx*phi", "iqyphi = iqy*phi", "lapphi = -q^2*phi",
+         "vx*eta*q^2 = -k*iqxphi*lapphi - k*iqx^2*1/q^2*iqxphi*lapphi - k*iqx*iqy*1/q^2*iqyphi*lapphi",
+         "vy*eta*q^2 = -k*iqyphi*lapphi - k*iqy^2*1/q^2*iqyphi*lapphi - k*iqx*iqy*1/q^2*iqxphi*lapphi"],
+    noises=[("phi", "2*T")])
+
+
+def test_modelh_1024_full_size():
+    n = 1024
+    init = {"phi": init_field(n * n, -0.1, 0.1)}
+    e, r = build_pair((n, n, 1), 0.01, MODEL_H["fields"], MODEL_H["params"], MODEL_H["eqs"], MODEL_H["noises"],
+                      init)
+    e.advanceTime(200)
+    r.advance(200)
+    errs = {name: rel_l2(e.getReal(name), r.real_field(name)) for name, _ in MODEL_H["fields"]}
+    e.close()
+    print("model H 1024^2, 200 steps: " + ", ".join("%s %.2e" % kv for kv in errs.items()))
+    assert max(errs.values()) < 5e-5
+
+
+def radial_structure_factor(phi, nbins=48):
+    f = np.abs(np.fft.fft2(phi - phi.mean())) ** 2 / phi.size
+    n = phi.shape[0]
+    k = np.fft.fftfreq(n) * n
+    kr = np.sqrt(k[:, None] ** 2 + k[None, :] ** 2)
+    b = np.minimum((kr / (n / 2) * nbins).astype(int), nbins)
+    s = np.bincount(b.ravel(), f.ravel(), nbins + 1)[:nbins]
+    c = np.bincount(b.ravel(), None, nbins + 1)[:nbins]
+    return s / np.maximum(c, 1)
+
+
+def test_ch2d_256_whole_run():
+    n, steps = 256, 10000
+    init = {"phi": init_field(n * n, -0.1, 0.1)}
+    e, r = build_pair((n, n, 1), 0.01, [("phi", True)], {"a": -1.0, "b": 1.0, "k": 1.0}, [CH_EQ], [], init)
+    errs = []
+    for chunk in (1000, 1000, 8000):
+        e.advanceTime(chunk)
+        r.advance(chunk)
+        errs.append(rel_l2(e.getReal("phi"), r.real_field("phi")))
+    got = e.getReal("phi").reshape(n, n).astype(np.float64)
+    ref = r.real_field("phi").reshape(n, n)
+    e.close()
+    print("2D CH 256^2: rel L2 after 1000 / 2000 / 10000 steps: %.2e / %.2e / %.2e" % tuple(errs))
+    # up to t = 10 the runs agree closely; the drift afterwards is the spinodal
+    # amplification of rounding, bounded here
+    assert errs[0] < 2e-5
+    assert errs[1] < 3e-4
+    assert errs[2] < 0.5
+    # what the drift leaves intact: conserved mean, structure factor, distribution
+    assert abs(got.mean() - ref.mean()) < 1e-5
+    sg, sr = radial_structure_factor(got), radial_structure_factor(ref)
+    main = sr > 0.05 * sr.max()
+    assert np.abs(sg[main] / sr[main] - 1).max() < 0.1
+    hg, _ = np.histogram(got, 40, (-1.2, 1.2))
+    hr, _ = np.histogram(ref, 40, (-1.2, 1.2))
+    assert np.abs(hg - hr).sum() / hr.sum() < 0.05

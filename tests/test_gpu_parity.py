@@ -86,12 +86,14 @@ CH = ([("phi", 1)], {"a": -1.0, "b": 1.0, "k": 1.0},
 # the reference's own known-answer tests, through this library (tests/tests.cpp:64-422)
 @pytest.mark.parametrize("dim", [1, 2, 3])
 def test_reference_init_goldens(dim):
+    # the library's own evolver::initializeDroplet (src/initializers.cpp:142-177), called
+    # through the C-ABI with the reference test's arguments (tests/tests.cpp:64-189), then
+    # uploaded, transformed and read back by the engine
     import cupss_gb300 as c
     shape = {1: (16, 1, 1), 2: (16, 16, 1), 3: (16, 16, 16)}[dim]
     e = c.Evolver(True, *shape, dt=1.0, write_every=1)
     e.createField("phi", True)
-    init = droplet(shape, 0, 1, 16 / 8, 4, 8, 8 if dim > 1 else 0, 0)
-    e.setReal("phi", init)
+    e.initializeDroplet("phi", 0, 1, 16 / 8, 4, 8, 8 if dim > 1 else 0, 0)
     e.prepareProblem()
     got = e.getReal("phi").ravel()
     assert np.abs(got - GOLD["phi_%dd" % dim]).max() < 1e-4

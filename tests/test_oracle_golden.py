@@ -77,3 +77,14 @@ def test_philox_known_answer():
     assert [int(v) for v in out] == [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]
     out = philox4x32_10(0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344, 0xa4093822, 0x299f31d0)
     assert [int(v) for v in out] == [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1]
+
+
+@pytest.mark.parametrize("shape", [(16, 1, 1), (2, 1, 1), (8, 8, 1), (1024, 2, 1), (4, 4, 4), (16, 8, 4),
+                                   (64, 32, 16)])
+def test_noise_c_restatement_equals_numpy(shape):
+    # oracle/noise.c (the fast path the tests use) against the numpy definition
+    from oracle import philox
+    assert philox._c_lib() is not None, "oracle/noise.c did not build"
+    a = philox.fourier_noise(*shape, 0x0123456789ABCDEF, 11, 2)
+    b = philox.fourier_noise_numpy(*shape, 0x0123456789ABCDEF, 11, 2)
+    assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max()

@@ -160,20 +160,26 @@ class _SolverView:
         return self.lib.cupssgb_solver_launch_count(self.h)
 
 
-def l2_note(wl):
-    """Working set of the step against the L2: packed half spectra of 4 B per grid point,
-    two state arrays and one dealiased channel per field (3D: one more for the z inverse),
-    one array per distinct product, and the real and spectral scratch arrays."""
+def device_bytes_estimate(wl):
+    """Device arrays of the step, 4 B per grid point each (packed half spectra): two states
+    and one dealiased channel per field (3D grids in the row-pass form keep a second one
+    for the z inverse; the xy-plane pass of square planes up to 256^2 needs none), one
+    product spectrum per distinct product, the real and spectral scratch arrays."""
     sx, sy, sz = wl["shape"]
     arr = 4.0 * sx * sy * sz
     nf = len(wl.get("fields", [None]))
-    ws = arr * (3 * nf + (nf if sz > 1 else 0) + wl.get("products", 1) + 2)
+    plane = sz > 1 and sx == sy and sx <= 256 and "fields" not in wl
+    return arr * (3 * nf + (nf if sz > 1 and not plane else 0) + wl.get("products", 1) + 2)
+
+
+def l2_note(dev_bytes):
+    """Working set of the step against the 126 MB L2."""
     l2 = 126e6
-    if ws > l2:
+    if dev_bytes > l2:
         return "working set about %.0f MB (states x2, dealiased copies, product spectra), larger than the " \
-               "126 MB L2" % (ws / 1e6)
+               "126 MB L2" % (dev_bytes / 1e6)
     return "working set about %.0f MB, within the 126 MB L2: the step runs L2-resident (timed without a " \
-           "flush)" % (ws / 1e6)
+           "flush)" % (dev_bytes / 1e6)
 
 
 def kernel_bytes(kind, wl):
@@ -195,7 +201,9 @@ def kernel_bytes(kind, wl):
         fx = min(Lx, (mx // W + 1) * W) / Lx
         fxi = min(Lx, (mx // Wi + 1) * Wi) / Lx
         fy = min(sy // 2, sy // 4 + 1) / (sy // 2)
+        rows = (2 * (sy // 4) + 1) / sy   # unmasked rows |n_y| <= sy/4 of H'
         return {"turnaround_z": 3 * arr + fx * fy * arr,     # read G'', read/write state, write H'
+                "plane_pass": cols * rows * arr + arr,       # read H' (unmasked columns and rows), write G''
                 "line_inv_y": fxi * fy * arr + fxi * arr,    # read H' (unmasked rows), write H
                 "row_pass": cols * arr + arr,                # read H (unmasked columns), write G'
                 "line_fwd_y": 2 * arr}[kind]                 # G' -> G''
@@ -590,8 +598,7 @@ def main():
         noise = " + conserved noise T=0.01" if "q^2" in wl["noise"][0][1] else " + noise T=%g" % wl["params"]["T"]
     cfg = {"workload": "%s: %dx%dx%d %s%s, dt=%g, FP32" % (args.workload, sx, sy, sz, system, noise, wl["dt"]),
         "grid": [sx, sy, sz], "equation": wl["eqs"][0], "noise": wl["noise"][0][1] if wl["noise"] else None,
-        "full_solve_steps": wl["solve_steps"],
-        "l2": l2_note(wl),
+        "full_solve_steps": wl["solve_steps"], "l2": l2_note(device_bytes_estimate(wl)),
         "parallelism": "replicas" if ws > 1 else "single GPU"}
 
     if args.impl == "reference":

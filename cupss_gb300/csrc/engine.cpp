@@ -33,6 +33,7 @@ Solver::Solver(int sx, int sy, int sz, float dx, float dy, float dz, float dt)
   if (const char* w = std::getenv("CUPSSGB_TURN_W")) turn_w_ = std::atoi(w);
   if (const char* b = std::getenv("CUPSSGB_TURN_WARPS")) turn_warps_ = std::max(1, std::atoi(b));
   if (const char* d = std::getenv("CUPSSGB_PDL")) pdl_ = std::string(d) != "0";
+  if (const char* d = std::getenv("CUPSSGB_PLANE")) plane_env_ = std::string(d) != "0";
   if (!pow2(sx) || sx < 2 || sx > 2048 || !pow2(sy) || sy > 1024 || !pow2(sz) || sz > 1024)
     throw Error(kErrUnsupported,
                 "grid sizes must be powers of two: 2 <= sx <= 2048, 1 <= sy, sz <= 1024");
@@ -222,11 +223,12 @@ void Solver::prepare() {
   chan_.assign(F, nullptr);
   chanz_.assign(F, nullptr);
   par_.assign(F, 0);
+  plane_ = decide_plane();
   for (int f = 0; f < F; ++f) {
     state_[0][f] = (float2*)dalloc(hall * sizeof(float2));
     state_[1][f] = (float2*)dalloc(hall * sizeof(float2));
     if (alias_order_[f] > 1) {
-      chan_[f] = (float2*)dalloc(hall * sizeof(float2));
+      if (!plane_) chan_[f] = (float2*)dalloc(hall * sizeof(float2));
       if (dim_ == 3) chanz_[f] = (float2*)dalloc(hall * sizeof(float2));
     }
   }
@@ -541,6 +543,59 @@ void Solver::channel_from_state(int f, float2* dst) {
   }
 }
 
+// Masked, 1/N-scaled state, z-inverted: the layout the turnaround leaves for the plane
+// pass (x and y spectral, z positional).
+void Solver::channelz_from_state(int f, float2* dst) {
+  MaskParams mp;
+  mp.sx = sx_;
+  mp.sy = sy_;
+  mp.sz = sz_;
+  mp.Lx = Lx_;
+  mp.xlim = sx_ / (alias_order_[f] + 1);
+  mp.ylim = sy_ / (alias_order_[f] + 1);
+  mp.zlim = sz_ / (alias_order_[f] + 1);
+  mp.scale = 1.0f / (float)npoints();
+  mp.spec = state_[par_[f]][f];
+  mp.out = dst;
+  check(launch_mask(mp, stream_), "mask spectrum");
+  ++launches_;
+  line_fwd_inv(kGeoZ3, kModeInv, dst, dst, Lx_);
+}
+
+bool Solver::plane_phase(const Phase& P) const {
+  if (dim_ != 3 || P.xin.size() != 1 || P.products.size() != 1) return false;
+  const int g = P.xin[0];
+  const int nc = std::min(Lx_, sx_ / (alias_order_[g] + 1) + 1);
+  return plane_pass_shape(Lx_, sy_, nc, nullptr, nullptr) > 0;
+}
+
+bool Solver::decide_plane() const {
+  if (dim_ != 3 || !plane_env_) return false;
+  bool any = false;
+  for (const Phase& P : phases_) {
+    if (P.products.empty()) continue;
+    if (!plane_phase(P)) return false;
+    any = true;
+  }
+  return any;
+}
+
+// A real-space callback can give a dealiased field content at every wavenumber, which
+// the plane store is not sized for: the solver goes back to the row-pass form, whose
+// channels are the y-inverses of the plane-pass channels.
+void Solver::leave_plane_mode() {
+  if (!plane_) return;
+  const size_t hall = half_ * (size_t)nmem_;
+  for (int f = 0; f < nfields(); ++f)
+    if (alias_order_[f] > 1 && !chan_[f]) {
+      chan_[f] = (float2*)dalloc(hall * sizeof(float2));
+      line_fwd_inv(kGeoY3, kModeInv, chanz_[f], chan_[f], sx_ / (alias_order_[f] + 1), batch_,
+                   sy_ / (alias_order_[f] + 1) + 1);
+    }
+  plane_ = false;
+  invalidate_graphs();
+}
+
 void Solver::set_fourier_device(int f, const float2* full) {
   if (!prepared_) throw Error(kErrState, "set_fourier before prepare");
   if (f < 0 || f >= nfields()) throw Error(kErrInvalid, "bad field index");
@@ -553,7 +608,10 @@ void Solver::set_fourier_device(int f, const float2* full) {
   cp.spec = state_[par_[f]][f];
   check(launch_compress(cp, stream_), "compress spectrum");
   ++launches_;
-  if (alias_order_[f] > 1) channel_from_state(f, chan_[f]);
+  if (alias_order_[f] > 1) {
+    if (plane_) channelz_from_state(f, chanz_[f]);
+    else channel_from_state(f, chan_[f]);
+  }
 }
 
 void Solver::set_real_pairs_device(int f, const float2* real, const float2* dealiased) {
@@ -565,10 +623,14 @@ void Solver::set_real_pairs_device(int f, const float2* real, const float2* deal
   if (alias_order_[f] > 1) {
     // the channel is the x spectrum scaled by 1/sx (see channel_from_state)
     if (dealiased) {
+      leave_plane_mode();
       row_pass_simple(kXInRealPair, dealiased, kXOutSpectral, chan_[f], 1.0f / (float)sx_);
       chan_wide_[f] = 1;
+    } else if (plane_) {
+      channelz_from_state(f, chanz_[f]);
+    } else {
+      channel_from_state(f, chan_[f]);
     }
-    else channel_from_state(f, chan_[f]);
   }
 }
 
@@ -768,8 +830,29 @@ std::vector<std::string> Solver::generated_sources() {
 
 void Solver::run_phase(Phase& P) {
   if (P.fields.empty()) return;
+  // ---- xy-plane pass (3D, one channel, one product): the product plane by plane ----
+  if (!P.products.empty() && plane_) {
+    const int g = P.xin[0];
+    PlaneParams pp;
+    std::memset(&pp, 0, sizeof(pp));
+    pp.nc = std::min(Lx_, sx_ / (alias_order_[g] + 1) + 1);
+    pp.ykeep = sy_ / (alias_order_[g] + 1) + 1;
+    size_t smem = 0;
+    if (plane_pass_shape(Lx_, sy_, pp.nc, &pp.ps, &smem) <= 0) throw Error(kErrUnsupported, "plane pass shape");
+    pp.order = (int)P.products[0].size();
+    pp.out_scale = 1.f;
+    pp.in = chanz_[g];
+    pp.out = P.prodbuf[0];
+    pp.tw = tw_;
+    pp.members = members_d_;
+    if (batch_) pp.mstride = half_;
+    mark_begin();
+    check(launch_plane_pass(pp, Lx_, sy_, sz_, batch_ ? mspan_ : 1, stream_, pdl_), "plane pass");
+    mark_end("plane_pass");
+    ++launches_;
+  }
   // ---- row pass: real-space products of the dealiased copies ----
-  if (!P.products.empty()) {
+  if (!P.products.empty() && !plane_) {
     XParams x;
     std::memset(&x, 0, sizeof(x));
     x.Lx = Lx_;
@@ -846,7 +929,7 @@ void Solver::run_phase(Phase& P) {
   mark_end(dim_ == 3 ? "turnaround_z" : "turnaround_y");
   ++launches_;
   for (int f : P.fields) par_[f] ^= 1;
-  if (dim_ == 3 && any_chan) {
+  if (dim_ == 3 && any_chan && !plane_) {
     for (int f : P.fields)
       if (alias_order_[f] > 1) {
         mark_begin();

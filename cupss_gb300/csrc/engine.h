@@ -173,6 +173,12 @@ class Solver {
                     int lkeep = 0, bool pdl = false);
   // real values of field f (member m) into dst (the real scratch array when null)
   void to_real_scratch(int f, int m, float* dst = nullptr);
+  // 3D: phases whose products are one channel's power run the xy-plane pass (plane.cuh)
+  // in place of a row pass and two y passes; decided at prepare (plane_)
+  bool plane_phase(const Phase& P) const;
+  bool decide_plane() const;
+  void leave_plane_mode();                       // back to the row-pass form (see set_real_pairs_device)
+  void channelz_from_state(int f, float2* dst);  // masked state / N, z-inverted (plane-pass input)
   void step_once(uint32_t off, bool tick);
   // batches
   void check_member(int m) const;
@@ -207,6 +213,8 @@ class Solver {
   int turn_warps_ = 16;       // resident warps per SM the generated turnaround's registers are sized for
   bool tuning_ = false;       // autotune in progress: run the width-generic generated kernel
   bool pdl_ = true;           // step kernels use programmatic dependent launch
+  bool plane_ = false;        // 3D products by the xy-plane pass (see plane_phase)
+  bool plane_env_ = true;     // CUPSSGB_PLANE=0 turns the plane pass off
   long long step_ = 0;
   long long launches_ = 0;
   size_t dev_bytes_ = 0;
@@ -229,8 +237,8 @@ class Solver {
   float2* tw_ = nullptr;
   std::vector<float2*> state_[2];
   std::vector<int> par_;
-  std::vector<float2*> chan_;    // row-pass input (x spectrum, y/z positional)
-  std::vector<float2*> chanz_;   // 3D: z-inverse output before the y-inverse
+  std::vector<float2*> chan_;    // row-pass input (x spectrum, y/z positional); null in plane mode
+  std::vector<float2*> chanz_;   // 3D: z-inverse output (the plane pass's input, or the y-inverse's)
   float* scratch_real_ = nullptr;
   float2* scratch_spec_ = nullptr;
   float2* scratch_full_ = nullptr;   // reference-layout full spectrum, allocated on first use

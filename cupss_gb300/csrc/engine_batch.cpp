@@ -258,9 +258,10 @@ size_t Solver::estimate_bytes(int members) {
   if (!prepared_) build_plan();
   const size_t half = (size_t)Lx_ * sy_ * sz_, arr = half * sizeof(float2) * (size_t)members;
   size_t b = 2 * 2048 * sizeof(float2) + npoints() * sizeof(float) + half * sizeof(float2);   // tables, scratch
+  const bool plane = prepared_ ? plane_ : decide_plane();
   for (int f = 0; f < nfields(); ++f) {
     b += 2 * arr;
-    if (alias_order_[f] > 1) b += (dim_ == 3 ? 2 : 1) * arr;
+    if (alias_order_[f] > 1) b += (dim_ == 3 && !plane ? 2 : 1) * arr;
   }
   for (const Phase& P : phases_) b += P.products.size() * arr;
   if (members > 1 || batch_) b += (size_t)members * (sizeof(MemberK) + 2 * kMemberVals * sizeof(float));

@@ -131,6 +131,20 @@ struct XParams {
   const MemberK* members;           // null for a single system
 };
 
+// xy-plane pass of a 3D phase (plane.cuh): product of one channel, plane by plane.
+struct PlaneParams {
+  int nc;             // input columns kx' < nc carry content
+  int ykeep;          // input rows with |n_y| >= ykeep are known zero (ykeep > sy/2: every row is read)
+  int ps;             // plane-store pitch in float2 (>= max(nc, Lx/C), = 8 mod 16)
+  int order;          // power of the real values (product size)
+  float out_scale;    // multiplies every product value
+  const float2* in;   // H'(kx', ky, z) at ((z*sy + ky)*Lx + kx'): x and y spectral, z positional
+  float2* out;        // G''(kx', ky, z), same layout
+  const float2* tw;
+  size_t mstride;     // batches: member z at blockIdx.z * mstride elements
+  const MemberK* members;
+};
+
 struct ExpandParams {
   int sx, sy, sz, Lx;
   const float2* spec;   // packed half spectrum, fully transformed

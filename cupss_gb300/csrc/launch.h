@@ -8,17 +8,18 @@
 
 namespace cupssgb {
 
-// Raises a kernel's dynamic shared-memory limit to 220 KiB on the current device.  The
-// attribute belongs to one device, so `done` records, one bit per device ordinal, the
-// devices where it is set; the bit is set after a successful call, and two threads that
-// race both make the (idempotent) call.
-inline cudaError_t raise_smem_limit(const void* kernel, std::atomic<unsigned long long>& done) {
+// Raises a kernel's dynamic shared-memory limit (220 KiB unless given) on the current
+// device.  The attribute belongs to one device, so `done` records, one bit per device
+// ordinal, the devices where it is set; the bit is set after a successful call, and two
+// threads that race both make the (idempotent) call.
+inline cudaError_t raise_smem_limit(const void* kernel, std::atomic<unsigned long long>& done,
+                                    int bytes = 220 * 1024) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   const unsigned long long bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
   if (bit && (done.load(std::memory_order_acquire) & bit)) return cudaSuccess;
-  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess && bit) done.fetch_or(bit, std::memory_order_acq_rel);
   return e;
 }
@@ -59,6 +60,13 @@ bool turn_split_form(int L);
 // CUPSSGB_SPLIT=0/1 forces the four-step / split form of lines of 512 and 1024 points in
 // the row pass and the generated turnaround (-1: not set, the automatic choice)
 int split_override();
+
+// xy-plane pass of a 3D phase with one channel and one product (plane.cuh), over the sz
+// planes of nz batch members.  plane_pass_shape: 0 when the grid (Lx = sx/2, sy) has no
+// plane-pass instantiation or its plane does not fit on chip, else the cluster size, and
+// *ps the plane-store pitch for nc input columns.
+int plane_pass_shape(int Lx, int sy, int nc, int* ps, size_t* smem);
+cudaError_t launch_plane_pass(const PlaneParams& p, int Lx, int sy, int sz, int nz, cudaStream_t st, bool pdl);
 
 cudaError_t launch_expand(const ExpandParams& p, cudaStream_t st);
 cudaError_t launch_compress(const CompressParams& p, cudaStream_t st);

@@ -838,7 +838,8 @@ void Solver::run_phase(Phase& P) {
     pp.nc = std::min(Lx_, sx_ / (alias_order_[g] + 1) + 1);
     pp.ykeep = sy_ / (alias_order_[g] + 1) + 1;
     size_t smem = 0;
-    if (plane_pass_shape(Lx_, sy_, pp.nc, &pp.ps, &smem) <= 0) throw Error(kErrUnsupported, "plane pass shape");
+    const int cl = plane_pass_shape(Lx_, sy_, pp.nc, &pp.ps, &smem);
+    if (cl <= 0) throw Error(kErrUnsupported, "plane pass shape");
     pp.order = (int)P.products[0].size();
     pp.out_scale = 1.f;
     pp.in = chanz_[g];
@@ -847,7 +848,7 @@ void Solver::run_phase(Phase& P) {
     pp.members = members_d_;
     if (batch_) pp.mstride = half_;
     mark_begin();
-    check(launch_plane_pass(pp, Lx_, sy_, sz_, batch_ ? mspan_ : 1, stream_, pdl_), "plane pass");
+    check(launch_plane_pass(pp, Lx_, sy_, sz_, batch_ ? mspan_ : 1, cl, stream_, pdl_), "plane pass");
     mark_end("plane_pass");
     ++launches_;
   }

@@ -1,4 +1,6 @@
 // xy-plane pass instantiations and dispatch by (Lx = sx/2, sy).
+#include <cstdlib>
+
 #include "launch.h"
 #include "plane.cuh"
 
@@ -57,14 +59,33 @@ template <int LX, int LY, int C>
 constexpr Shape shape_of() {
   return Shape{LX, LY, C, PlaneCfg<LX, LY, C>::CX, PlaneCfg<LX, LY, C>::T_F2};
 }
-constexpr Shape kShapes[] = {shape_of<8, 16, 1>(), shape_of<16, 32, 1>(), shape_of<32, 64, 1>(),
-                             shape_of<64, 128, 1>(), shape_of<128, 256, 2>()};
+constexpr Shape kShapes[] = {shape_of<8, 16, 1>(),   shape_of<16, 32, 1>(),  shape_of<32, 64, 1>(),
+                             shape_of<64, 128, 1>(), shape_of<64, 128, 2>(), shape_of<128, 256, 2>(),
+                             shape_of<128, 256, 4>()};
+
+// cluster size of a plane shape: the default (the first instantiated), or `want` when
+// that one is instantiated too
+int cluster_of(int Lx, int sy, int want) {
+  int first = 0;
+  for (const Shape& s : kShapes)
+    if (s.lx == Lx && s.ly == sy) {
+      if (!first) first = s.c;
+      if (s.c == want) return want;
+    }
+  return first;
+}
 
 }  // namespace
 
-int plane_pass_shape(int Lx, int sy, int nc, int* ps, size_t* smem) {
+int plane_cluster_override() {
+  const char* e = std::getenv("CUPSSGB_PLANE_C");
+  return e ? std::atoi(e) : 0;
+}
+
+int plane_pass_shape(int Lx, int sy, int nc, int* ps, size_t* smem, int want_c) {
+  const int c = cluster_of(Lx, sy, want_c > 0 ? want_c : plane_cluster_override());
   for (const Shape& s : kShapes)
-    if (s.lx == Lx && s.ly == sy) {
+    if (s.lx == Lx && s.ly == sy && s.c == c) {
       const int pitch = store_pitch(nc, s.cx);
       const size_t bytes = ((size_t)s.ly * pitch + s.t_f2) * sizeof(float2);
       if (bytes > (size_t)kMaxSmem) return 0;
@@ -75,12 +96,15 @@ int plane_pass_shape(int Lx, int sy, int nc, int* ps, size_t* smem) {
   return 0;
 }
 
-cudaError_t launch_plane_pass(const PlaneParams& p, int Lx, int sy, int sz, int nz, cudaStream_t st, bool pdl) {
-  if (Lx == 8 && sy == 16) return launch_t<8, 16, 1>(p, sz, nz, st, pdl);
-  if (Lx == 16 && sy == 32) return launch_t<16, 32, 1>(p, sz, nz, st, pdl);
-  if (Lx == 32 && sy == 64) return launch_t<32, 64, 1>(p, sz, nz, st, pdl);
-  if (Lx == 64 && sy == 128) return launch_t<64, 128, 1>(p, sz, nz, st, pdl);
-  if (Lx == 128 && sy == 256) return launch_t<128, 256, 2>(p, sz, nz, st, pdl);
+cudaError_t launch_plane_pass(const PlaneParams& p, int Lx, int sy, int sz, int nz, int c, cudaStream_t st,
+                              bool pdl) {
+  if (Lx == 8 && sy == 16 && c == 1) return launch_t<8, 16, 1>(p, sz, nz, st, pdl);
+  if (Lx == 16 && sy == 32 && c == 1) return launch_t<16, 32, 1>(p, sz, nz, st, pdl);
+  if (Lx == 32 && sy == 64 && c == 1) return launch_t<32, 64, 1>(p, sz, nz, st, pdl);
+  if (Lx == 64 && sy == 128 && c == 1) return launch_t<64, 128, 1>(p, sz, nz, st, pdl);
+  if (Lx == 64 && sy == 128 && c == 2) return launch_t<64, 128, 2>(p, sz, nz, st, pdl);
+  if (Lx == 128 && sy == 256 && c == 2) return launch_t<128, 256, 2>(p, sz, nz, st, pdl);
+  if (Lx == 128 && sy == 256 && c == 4) return launch_t<128, 256, 4>(p, sz, nz, st, pdl);
   return cudaErrorInvalidValue;
 }
 

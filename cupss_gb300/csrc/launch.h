@@ -62,11 +62,14 @@ bool turn_split_form(int L);
 int split_override();
 
 // xy-plane pass of a 3D phase with one channel and one product (plane.cuh), over the sz
-// planes of nz batch members.  plane_pass_shape: 0 when the grid (Lx = sx/2, sy) has no
-// plane-pass instantiation or its plane does not fit on chip, else the cluster size, and
-// *ps the plane-store pitch for nc input columns.
-int plane_pass_shape(int Lx, int sy, int nc, int* ps, size_t* smem);
-cudaError_t launch_plane_pass(const PlaneParams& p, int Lx, int sy, int sz, int nz, cudaStream_t st, bool pdl);
+// planes of nz batch members, c CTAs per plane.  plane_pass_shape: 0 when the grid
+// (Lx = sx/2, sy) has no plane-pass instantiation or its plane does not fit on chip, else
+// the cluster size (want_c when that one is instantiated, else the shape's default;
+// CUPSSGB_PLANE_C sets want_c when it is 0), with *ps the plane-store pitch for nc input
+// columns and *smem the dynamic shared memory of one CTA.
+int plane_pass_shape(int Lx, int sy, int nc, int* ps, size_t* smem, int want_c = 0);
+cudaError_t launch_plane_pass(const PlaneParams& p, int Lx, int sy, int sz, int nz, int c, cudaStream_t st,
+                              bool pdl);
 
 cudaError_t launch_expand(const ExpandParams& p, cudaStream_t st);
 cudaError_t launch_compress(const CompressParams& p, cudaStream_t st);

@@ -23,7 +23,7 @@ SOURCES = [
     "k_row.cu", "k_plane.cu", "k_misc.cu", "noalloc.cu",
     "engine.cpp", "engine_batch.cpp", "capi.cpp", "jit.cpp",
     "host_parser.cpp", "host_evolver.cpp", "host_field_term.cpp", "host_init.cpp", "host_utils.cpp",
-    "host_ir.cpp", "host_ensemble.cpp", "host_server.cpp", "host_output.cpp",
+    "host_ir.cpp", "host_ensemble.cpp", "host_server.cpp", "host_output.cpp", "tune_cache.cpp",
 ]
 
 

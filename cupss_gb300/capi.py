@@ -104,6 +104,9 @@ SIGNATURES = {
     "cupssgb_host_free": (_I, [_P]),
     "cupssgb_set_device": (_I, [_I]),
     "cupssgb_device_info": (_I, [C.c_char_p, _I]),
+    "cupssgb_tune_cache_path": (_I, [C.c_char_p, _I]),
+    "cupssgb_tune_cache_lookup": (_I, [_S, C.c_char_p, _I]),
+    "cupssgb_tune_cache_store": (_I, [_S, _S]),
     "cupssgb_solver_snapshot_real": (_I, [_P, _I, _P, _P]),
     "cupssgb_evolver_flush_output": (_I, [_P]),
     "cupssgb_evolver_create_from_file": (_I, [_P, _S]),

@@ -13,6 +13,7 @@
 #include "engine.h"
 #include "host_common.h"
 #include "jit.h"
+#include "tune_cache.h"
 
 struct cupssgb_solver {
   cupssgb::Solver* s;
@@ -396,6 +397,24 @@ int cupssgb_solver_snapshot_real(cupssgb_solver* s, int field, float* host_real,
     s->s->snapshot_real(field, host_real, (cudaEvent_t)done_event);
     return 0;
   });
+}
+
+int cupssgb_tune_cache_path(char* buf, int buflen) {
+  return copy_out(cupssgb::tune_cache_path(), buf, buflen);
+}
+
+int cupssgb_tune_cache_lookup(const char* key, char* value, int buflen) {
+  NEED(key);
+  std::string v;
+  if (!cupssgb::tune_cache_lookup(key, &v)) return fail(CUPSSGB_ERR_INVALID, std::string("no entry for ") + key);
+  return copy_out(v, value, buflen);
+}
+
+int cupssgb_tune_cache_store(const char* key, const char* value) {
+  NEED(key);
+  NEED(value);
+  if (!cupssgb::tune_cache_store(key, value)) return fail(CUPSSGB_ERR_INVALID, "tune cache not written");
+  return 0;
 }
 
 int cupssgb_set_device(int device) {

@@ -33,7 +33,7 @@ Solver::Solver(int sx, int sy, int sz, float dx, float dy, float dz, float dt)
   if (const char* w = std::getenv("CUPSSGB_TURN_W")) turn_w_ = std::atoi(w);
   if (const char* b = std::getenv("CUPSSGB_TURN_WARPS")) turn_warps_ = std::max(1, std::atoi(b));
   if (const char* d = std::getenv("CUPSSGB_PDL")) pdl_ = std::string(d) != "0";
-  if (const char* d = std::getenv("CUPSSGB_PLANE")) plane_env_ = std::string(d) != "0";
+  if (const char* d = std::getenv("CUPSSGB_PLANE")) plane_env_ = std::string(d) == "0" ? 0 : 1;
   if (!pow2(sx) || sx < 2 || sx > 2048 || !pow2(sy) || sy > 1024 || !pow2(sz) || sz > 1024)
     throw Error(kErrUnsupported,
                 "grid sizes must be powers of two: 2 <= sx <= 2048, 1 <= sy, sz <= 1024");
@@ -223,12 +223,14 @@ void Solver::prepare() {
   chan_.assign(F, nullptr);
   chanz_.assign(F, nullptr);
   par_.assign(F, 0);
-  plane_ = decide_plane();
+  // the plane pass is a candidate of the tuner; both forms keep their channel buffers
+  plane_ok_ = decide_plane();
+  plane_ = plane_ok_;
   for (int f = 0; f < F; ++f) {
     state_[0][f] = (float2*)dalloc(hall * sizeof(float2));
     state_[1][f] = (float2*)dalloc(hall * sizeof(float2));
     if (alias_order_[f] > 1) {
-      if (!plane_) chan_[f] = (float2*)dalloc(hall * sizeof(float2));
+      chan_[f] = (float2*)dalloc(hall * sizeof(float2));
       if (dim_ == 3) chanz_[f] = (float2*)dalloc(hall * sizeof(float2));
     }
   }
@@ -273,7 +275,7 @@ void Solver::prepare() {
       int nslots = 0;
       bool any_chan = false;
       fill_turn(P, p, nslots, any_chan);
-      p.W = P.tuned_w > 0 ? P.tuned_w : pick_w(L, nl, nslots, turn_rows(), turn_split());
+      p.W = P.tuned_w > 0 ? P.tuned_w : pick_w(L, nl, nslots, turn_rows(), phase_split(P));
       if (turn_w_ > 0 && turn_w_ < p.W && P.tuned_w <= 0) p.W = turn_w_;
       jit_kernel(turn_source(P, p, L, nl), "cupssgb_turn");
     }
@@ -294,8 +296,10 @@ static int sm_count() {
   return v;
 }
 
-bool Solver::turn_split() const {
-  return use_jit_ && turn_split_form(dim_ == 3 ? sz_ : sy_);
+bool Solver::phase_split(const Phase& P) const {
+  if (!use_jit_ || turn_len() < 512) return false;
+  if (P.tuned_split >= 0 && split_override() < 0) return P.tuned_split == 1;
+  return turn_split_form(turn_len());
 }
 
 int Solver::pick_w(int L, int nl, int nslots, int other, bool split) const {
@@ -570,7 +574,7 @@ bool Solver::plane_phase(const Phase& P) const {
 }
 
 bool Solver::decide_plane() const {
-  if (dim_ != 3 || !plane_env_) return false;
+  if (dim_ != 3 || plane_env_ == 0) return false;
   bool any = false;
   for (const Phase& P : phases_) {
     if (P.products.empty()) continue;
@@ -580,19 +584,21 @@ bool Solver::decide_plane() const {
   return any;
 }
 
-// A real-space callback can give a dealiased field content at every wavenumber, which
-// the plane store is not sized for: the solver goes back to the row-pass form, whose
-// channels are the y-inverses of the plane-pass channels.
-void Solver::leave_plane_mode() {
-  if (!plane_) return;
-  const size_t hall = half_ * (size_t)nmem_;
+// The row-pass channels are the y-inverses of the plane-pass channels.
+void Solver::sync_row_channels() {
   for (int f = 0; f < nfields(); ++f)
-    if (alias_order_[f] > 1 && !chan_[f]) {
-      chan_[f] = (float2*)dalloc(hall * sizeof(float2));
+    if (alias_order_[f] > 1)
       line_fwd_inv(kGeoY3, kModeInv, chanz_[f], chan_[f], sx_ / (alias_order_[f] + 1), batch_,
                    sy_ / (alias_order_[f] + 1) + 1);
-    }
+}
+
+// A real-space callback can give a dealiased field content at every wavenumber, which
+// the plane store is not sized for: the solver goes back to the row-pass form.
+void Solver::leave_plane_mode() {
+  if (!plane_) return;
+  sync_row_channels();
   plane_ = false;
+  plane_ok_ = false;
   invalidate_graphs();
 }
 
@@ -803,11 +809,12 @@ const std::string& Solver::turn_source(Phase& P, const LineParams& p, int L, int
     const PresK& q = p.pres[j];
     sig.insert(sig.end(), {q.q2n, q.iqx, q.iqy, q.iqz, q.invq});
   }
-  sig.push_back(turn_warps_);
+  sig.push_back(phase_warps(P));
+  sig.push_back(phase_split(P) ? 1 : 0);
   sig.push_back(batch_ ? 1 : 0);
   if (sig != P.jit_sig) {
     P.jit_sig = sig;
-    P.jit_src = jit_generate_turn(p, L, nl, turn_warps_, batch_);
+    P.jit_src = jit_generate_turn(p, L, nl, phase_warps(P), batch_, phase_split(P));
   }
   return P.jit_src;
 }
@@ -823,7 +830,7 @@ std::vector<std::string> Solver::generated_sources() {
     int nslots = 0;
     bool any_chan = false;
     fill_turn(P, p, nslots, any_chan);
-    out.push_back(jit_generate_turn(p, L, nl, turn_warps_, batch_));
+    out.push_back(jit_generate_turn(p, L, nl, phase_warps(P), batch_, phase_split(P)));
   }
   return out;
 }
@@ -838,7 +845,7 @@ void Solver::run_phase(Phase& P) {
     pp.nc = std::min(Lx_, sx_ / (alias_order_[g] + 1) + 1);
     pp.ykeep = sy_ / (alias_order_[g] + 1) + 1;
     size_t smem = 0;
-    const int cl = plane_pass_shape(Lx_, sy_, pp.nc, &pp.ps, &smem);
+    const int cl = plane_pass_shape(Lx_, sy_, pp.nc, &pp.ps, &smem, plane_c_);
     if (cl <= 0) throw Error(kErrUnsupported, "plane pass shape");
     pp.order = (int)P.products[0].size();
     pp.out_scale = 1.f;
@@ -900,7 +907,7 @@ void Solver::run_phase(Phase& P) {
   int nslots = 0;
   bool any_chan = false;
   fill_turn(P, p, nslots, any_chan);
-  p.W = pick_w(L, nl, nslots, turn_rows(), turn_split());
+  p.W = pick_w(L, nl, nslots, turn_rows(), phase_split(P));
   if (turn_w_ > 0 && turn_w_ < p.W) p.W = turn_w_;
   if (P.tuned_w > 0) p.W = P.tuned_w;
   p.members = members_d_;
@@ -920,9 +927,9 @@ void Solver::run_phase(Phase& P) {
     if (tuning_) ps.W = 0;
     const std::string& src = turn_source(P, ps, L, nl);
     cudaKernel_t k = jit_kernel(src, "cupssgb_turn");
-    dim3 block(p.W, line_threads(L, 1, 1, turn_split()), nl);
+    dim3 block(p.W, line_threads(L, 1, 1, phase_split(P)), nl);
     void* args[] = {(void*)&p};
-    LaunchCfg lc(grid, block, line_pass_smem(L, nl, p.W, nslots, turn_split()), stream_, pdl_);
+    LaunchCfg lc(grid, block, line_pass_smem(L, nl, p.W, nslots, phase_split(P)), stream_, pdl_);
     check(cudaLaunchKernelExC(&lc.cfg, (const void*)k, args), "turnaround (generated)");
   } else {
     check(launch_line_pass(p, nl, nslots, grid, stream_, pdl_), "turnaround");

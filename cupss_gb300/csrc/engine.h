@@ -150,8 +150,11 @@ class Solver {
     std::vector<int> term_slot;              // per (field, term) flattened: product slot or -1
     std::vector<int> jit_sig;                // structure of the last generated update program
     std::string jit_src;
-    int tuned_w = 0;                         // batches: autotuned turnaround tile width
-    std::vector<std::pair<int, double>> tune_ms;   // candidate W -> ms per launch
+    int tuned_w = 0;                         // autotuned turnaround tile width (0: pick_w's rule)
+    int tuned_warps = 0;                     // resident-warp target of its registers (0: the solver's)
+    int tuned_split = -1;                    // 512/1024-point lines: 1 split form, 0 four-step, -1 rule
+    bool tune_cached = false;                // the shape came from the tune cache
+    std::vector<std::pair<std::string, double>> tune_ms;   // candidate -> ms per phase run
   };
 
   void check(cudaError_t e, const char* what);
@@ -166,8 +169,14 @@ class Solver {
   // split: the lines use the split FFT form
   int pick_w(int L, int nl, int nslots, int other = 0, bool split = false) const;
   int turn_rows() const { return dim_ == 3 ? std::max(sy_ / 2, 1) : 1; }
-  // the turnaround runs the generated kernel with lines in the split FFT form
-  bool turn_split() const;
+  // the phase's turnaround runs the generated kernel with lines in the split FFT form
+  bool phase_split(const Phase& P) const;
+  int phase_warps(const Phase& P) const { return P.tuned_warps > 0 ? P.tuned_warps : turn_warps_; }
+  int turn_len() const { return dim_ == 3 ? sz_ : sy_; }
+  // autotuner: cache key of a phase, its value string, and applying a cached value
+  std::string tune_key(const Phase& P);
+  std::string tune_value(const Phase& P, double ms) const;
+  bool apply_tune_value(Phase& P, const std::string& v, int wmax_rule);
   // lkeep > 0: inverse-pass input positions with |n| >= lkeep along the line are zero
   void line_fwd_inv(int geo, int mode, const float2* in, float2* out, int xlimit, bool batch = false,
                     int lkeep = 0, bool pdl = false);
@@ -178,6 +187,8 @@ class Solver {
   bool plane_phase(const Phase& P) const;
   bool decide_plane() const;
   void leave_plane_mode();                       // back to the row-pass form (see set_real_pairs_device)
+  // keeps the row-pass channels current when the plane pass is switched off
+  void sync_row_channels();
   void channelz_from_state(int f, float2* dst);  // masked state / N, z-inverted (plane-pass input)
   void step_once(uint32_t off, bool tick);
   // batches
@@ -213,8 +224,10 @@ class Solver {
   int turn_warps_ = 16;       // resident warps per SM the generated turnaround's registers are sized for
   bool tuning_ = false;       // autotune in progress: run the width-generic generated kernel
   bool pdl_ = true;           // step kernels use programmatic dependent launch
-  bool plane_ = false;        // 3D products by the xy-plane pass (see plane_phase)
-  bool plane_env_ = true;     // CUPSSGB_PLANE=0 turns the plane pass off
+  bool plane_ok_ = false;     // every product phase can run the xy-plane pass (decide_plane)
+  bool plane_ = false;        // 3D products by the xy-plane pass: chosen by the tuner among plane_ok_
+  int plane_c_ = 0;           // CTAs per plane of the plane pass (0: the shape's default)
+  int plane_env_ = -1;        // CUPSSGB_PLANE: 0 never the plane pass, 1 always where it applies, unset: tuned
   long long step_ = 0;
   long long launches_ = 0;
   size_t dev_bytes_ = 0;
@@ -237,7 +250,7 @@ class Solver {
   float2* tw_ = nullptr;
   std::vector<float2*> state_[2];
   std::vector<int> par_;
-  std::vector<float2*> chan_;    // row-pass input (x spectrum, y/z positional); null in plane mode
+  std::vector<float2*> chan_;    // row-pass input (x spectrum, y/z positional)
   std::vector<float2*> chanz_;   // 3D: z-inverse output (the plane pass's input, or the y-inverse's)
   float* scratch_real_ = nullptr;
   float2* scratch_spec_ = nullptr;

@@ -10,11 +10,15 @@
 // replayed from CUDA graphs.  The turnaround tile width of each phase is picked at
 // prepare by timing the candidates on the batch itself.
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <sstream>
 
 #include "engine.h"
+#include "jit.h"
 #include "launch.h"
+#include "tune_cache.h"
 
 namespace cupssgb {
 
@@ -182,14 +186,24 @@ void Solver::zero_dynamic_buffers() {
   std::fill(par_.begin(), par_.end(), 0);
 }
 
-// Times each candidate tile width of every phase's turnaround on the solver itself
-// (one warm-up and three timed runs of the whole phase) and keeps the fastest.  The
-// phases run on the zeroed buffers of a freshly prepared solver; every buffer is
-// zeroed again afterwards and no step is counted.  Runs for single systems too: a 2D
-// grid has only Lx/W turnaround CTAs, so narrow tiles can win on large 2D grids.
+// Autotuner.  For every phase it times the launch shapes of the phase on the solver
+// itself (one warm-up and three timed runs of the whole phase per candidate) and keeps the
+// fastest, one dimension after the other (2-4 only from 2^20 grid points times members on):
+//   1. the turnaround's tile width W (up to four widths);
+//   2. the resident-warp target its registers are sized for (16 and 24 warps per SM);
+//   3. lines of 512 and 1024 points: the split or the four-step FFT form;
+//   4. 3D plane mode, the phase with the product: CTAs per plane of the xy-plane pass.
+// The phases run on the zeroed buffers of a freshly prepared solver; every buffer is
+// zeroed again afterwards and no step is counted.  The winners are stored in the tune
+// cache (tune_cache.cpp) under a key naming the GPU, the grid, the batch span and the
+// phase's update program, and a later solver with the same key takes them from there
+// without timing.  CUPSSGB_TUNE=0 skips all of it (rule-based shapes); CUPSSGB_TURN_W
+// fixes W.
 void Solver::autotune() {
-  const int L = (dim_ == 3) ? sz_ : sy_;
+  const int L = turn_len();
   const int nl = (dim_ == 3) ? 2 : 1;
+  const char* te = std::getenv("CUPSSGB_TUNE");
+  const bool tune_on = !(te && std::string(te) == "0");
   cudaEvent_t a, b;
   check(cudaEventCreate(&a), "cudaEventCreate");
   check(cudaEventCreate(&b), "cudaEventCreate");
@@ -207,25 +221,29 @@ void Solver::autotune() {
   }
   check(cudaMemcpyAsync(members_d_, all.data(), all.size() * sizeof(MemberK), cudaMemcpyHostToDevice, stream_),
         "member upload");
+  bool plane_tuned = false;
   for (Phase& P : phases_) {
     P.tune_ms.clear();
+    P.tune_cached = false;
     if (P.fields.empty()) continue;
     LineParams p;
     int nslots = 0;
     bool any_chan = false;
     fill_turn(P, p, nslots, any_chan);
-    const int wmax = pick_w(L, nl, nslots, 0, turn_split());
+    const int wmax = pick_w(L, nl, nslots, 0, phase_split(P));
     if (turn_w_ > 0) {
       P.tuned_w = std::min(turn_w_, wmax);
       continue;
     }
-    std::vector<int> cands;
-    for (int w = wmax; w >= 2 && cands.size() < 4; w /= 2) cands.push_back(w);
-    if (cands.empty()) cands.push_back(wmax);
-    double best = 1e30;
-    int best_w = wmax;
-    for (int w : cands) {
-      P.tuned_w = w;
+    if (!tune_on) continue;
+    const std::string key = tune_key(P);
+    std::string cached;
+    if (tune_cache_lookup(key, &cached) && apply_tune_value(P, cached, wmax)) {
+      P.tune_cached = true;
+      if (!P.products.empty()) plane_tuned = true;
+      continue;
+    }
+    auto time_phase = [&](const std::string& what) {
       run_phase(P);
       check(cudaEventRecord(a, stream_), "cudaEventRecord");
       for (int r = 0; r < 3; ++r) run_phase(P);
@@ -233,13 +251,71 @@ void Solver::autotune() {
       check(cudaEventSynchronize(b), "cudaEventSynchronize");
       float ms = 0.f;
       check(cudaEventElapsedTime(&ms, a, b), "cudaEventElapsedTime");
-      P.tune_ms.push_back({w, ms / 3.0});
+      P.tune_ms.push_back({what, ms / 3.0});
+      return ms / 3.0;
+    };
+    // 1. tile width
+    std::vector<int> cands;
+    for (int w = wmax; w >= 2 && cands.size() < 4; w /= 2) cands.push_back(w);
+    if (cands.empty()) cands.push_back(wmax);
+    double best = 1e30;
+    int best_w = wmax;
+    for (int w : cands) {
+      P.tuned_w = w;
+      const double ms = time_phase("W=" + std::to_string(w));
       if (ms < best) {
         best = ms;
         best_w = w;
       }
     }
     P.tuned_w = best_w;
+    // the other dimensions need kernels of their own (compiled at prepare); below 2^20
+    // grid points (times members) a step is launch-bound and W is all that is timed
+    const bool deep = (double)npoints() * mspan_ >= (double)(1 << 20);
+    if (use_jit_ && deep) {
+      // 2. resident-warp target (a kernel compiled for each)
+      const int w0 = phase_warps(P);
+      const int alt = w0 == 16 ? 24 : 16;
+      P.tuned_warps = alt;
+      const double ms = time_phase("warps=" + std::to_string(alt));
+      if (ms < best) best = ms;
+      else P.tuned_warps = w0;
+      // 3. FFT form of 512- and 1024-point lines (the width must suit the other form too)
+      if (L >= 512 && split_override() < 0) {
+        const bool s0 = phase_split(P);
+        P.tuned_split = s0 ? 0 : 1;
+        if (P.tuned_w <= pick_w(L, nl, nslots, 0, !s0)) {
+          const double ms2 = time_phase(std::string("split=") + (s0 ? "0" : "1"));
+          if (ms2 < best) best = ms2;
+          else P.tuned_split = s0 ? 1 : 0;
+        } else {
+          P.tuned_split = s0 ? 1 : 0;
+        }
+      }
+    }
+    // 4. 3D products: the xy-plane pass (each instantiated cluster size) or the row pass
+    //    with two y line passes (one choice per solver, made on its first product phase)
+    if (plane_ok_ && plane_env_ < 0 && deep && !P.products.empty() && !plane_tuned) {
+      plane_tuned = true;
+      const int g = P.xin[0];
+      const int nc = std::min(Lx_, sx_ / (alias_order_[g] + 1) + 1);
+      if (plane_cluster_override() <= 0) {
+        const int c0 = plane_pass_shape(Lx_, sy_, nc, nullptr, nullptr, plane_c_);
+        for (int c : {1, 2, 4, 8}) {
+          if (c == c0 || plane_pass_shape(Lx_, sy_, nc, nullptr, nullptr, c) != c) continue;
+          const int keep = plane_c_;
+          plane_c_ = c;
+          const double ms = time_phase("plane_c=" + std::to_string(c));
+          if (ms < best) best = ms;
+          else plane_c_ = keep;
+        }
+      }
+      plane_ = false;
+      const double ms = time_phase("plane=0");
+      if (ms < best) best = ms;
+      else plane_ = true;
+    }
+    tune_cache_store(key, tune_value(P, best));
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
@@ -253,15 +329,80 @@ void Solver::autotune() {
   check(cudaStreamSynchronize(stream_), "autotune");
 }
 
+// Cache key of a phase: the GPU (name and multiprocessors), the grid, the batch span, the
+// plane mode and a hash of the phase's width-generic update program at the default shape
+// (which fixes the structure of the update).  kTuneFormat changes when kernels change in
+// a way that makes old timings meaningless.
+std::string Solver::tune_key(const Phase& P) {
+  constexpr int kTuneFormat = 2;
+  int dev = 0;
+  check(cudaGetDevice(&dev), "cudaGetDevice");
+  cudaDeviceProp pr;
+  check(cudaGetDeviceProperties(&pr, dev), "cudaGetDeviceProperties");
+  std::string gpu = pr.name;
+  for (char& ch : gpu)
+    if (ch == ' ' || ch == '\t' || ch == '/') ch = '_';
+  LineParams p;
+  int nslots = 0;
+  bool any_chan = false;
+  fill_turn(P, p, nslots, any_chan);
+  p.W = 0;
+  const int L = turn_len();
+  const std::string src = jit_generate_turn(p, L, dim_ == 3 ? 2 : 1, turn_warps_, batch_, turn_split_form(L));
+  char h[17];
+  std::snprintf(h, sizeof(h), "%016llx", (unsigned long long)fnv1a64(src));
+  std::ostringstream os;
+  os << "v" << kTuneFormat << "/" << gpu << "/sm" << pr.multiProcessorCount << "/" << sx_ << "x" << sy_ << "x" << sz_
+     << "/m" << mspan_ << "/p" << P.id << "/plane" << (plane_ok_ ? 1 : 0) << "/jit" << (use_jit_ ? 1 : 0) << "/" << h;
+  return os.str();
+}
+
+std::string Solver::tune_value(const Phase& P, double ms) const {
+  std::ostringstream os;
+  os << "W=" << P.tuned_w << " warps=" << phase_warps(P) << " split=" << (phase_split(P) ? 1 : 0)
+     << " plane=" << (plane_ ? 1 : 0) << " plane_c=" << plane_c_ << " ms=" << ms;
+  return os.str();
+}
+
+bool Solver::apply_tune_value(Phase& P, const std::string& v, int wmax_rule) {
+  double w = 0, warps = 0, split = -1, pc = 0, pl = 0;
+  if (!tune_value_get(v, "W", &w) || !tune_value_get(v, "warps", &warps) || !tune_value_get(v, "split", &split) ||
+      !tune_value_get(v, "plane_c", &pc) || !tune_value_get(v, "plane", &pl))
+    return false;
+  const int L = turn_len();
+  const int nl = (dim_ == 3) ? 2 : 1;
+  LineParams p;
+  int nslots = 0;
+  bool any_chan = false;
+  fill_turn(P, p, nslots, any_chan);
+  const bool sp = use_jit_ && L >= 512 && split > 0.5;
+  const int wmax = use_jit_ ? pick_w(L, nl, nslots, 0, sp) : wmax_rule;
+  const int wi = (int)w;
+  if (wi < 1 || wi > wmax || (wi & (wi - 1)) != 0 || warps < 8 || warps > 64) return false;
+  int c = (int)pc;
+  if (plane_ok_ && plane_env_ < 0 && !P.products.empty()) {
+    if (pl > 0.5 && c > 0) {
+      const int g = P.xin[0];
+      const int nc = std::min(Lx_, sx_ / (alias_order_[g] + 1) + 1);
+      if (plane_pass_shape(Lx_, sy_, nc, nullptr, nullptr, c) != c) return false;
+      plane_c_ = c;
+    }
+    plane_ = pl > 0.5;
+  }
+  P.tuned_w = wi;
+  P.tuned_warps = (int)warps;
+  if (L >= 512) P.tuned_split = sp ? 1 : 0;
+  return true;
+}
+
 size_t Solver::estimate_bytes(int members) {
   if (members < 1) throw Error(kErrInvalid, "members >= 1");
   if (!prepared_) build_plan();
   const size_t half = (size_t)Lx_ * sy_ * sz_, arr = half * sizeof(float2) * (size_t)members;
   size_t b = 2 * 2048 * sizeof(float2) + npoints() * sizeof(float) + half * sizeof(float2);   // tables, scratch
-  const bool plane = prepared_ ? plane_ : decide_plane();
   for (int f = 0; f < nfields(); ++f) {
     b += 2 * arr;
-    if (alias_order_[f] > 1) b += (dim_ == 3 && !plane ? 2 : 1) * arr;
+    if (alias_order_[f] > 1) b += (dim_ == 3 ? 2 : 1) * arr;
   }
   for (const Phase& P : phases_) b += P.products.size() * arr;
   if (members > 1 || batch_) b += (size_t)members * (sizeof(MemberK) + 2 * kMemberVals * sizeof(float));
@@ -285,7 +426,9 @@ std::string Solver::tune_report() const {
     if (P.fields.empty()) continue;
     if (!first) os << ", ";
     first = false;
-    os << "\"phase" << P.id << "\": {\"W\": " << P.tuned_w << ", \"ms\": {";
+    os << "\"phase" << P.id << "\": {\"W\": " << P.tuned_w << ", \"warps\": " << phase_warps(P)
+       << ", \"split\": " << (phase_split(P) ? 1 : 0) << ", \"plane\": " << (plane_ ? 1 : 0)
+       << ", \"plane_c\": " << plane_c_ << ", \"cached\": " << (P.tune_cached ? "true" : "false") << ", \"ms\": {";
     for (size_t i = 0; i < P.tune_ms.size(); ++i)
       os << (i ? ", " : "") << "\"" << P.tune_ms[i].first << "\": " << P.tune_ms[i].second;
     os << "}}";

@@ -62,7 +62,7 @@ std::string keep_expr(int s, const PresK& p, bool* never) {
 
 }  // namespace
 
-std::string jit_generate_turn(const LineParams& p, int L, int NL, int warps, bool batched) {
+std::string jit_generate_turn(const LineParams& p, int L, int NL, int warps, bool batched, bool split_form) {
   // numerical values: the parameter block (one system) or the batch member's row
   auto pre = [&](int k) {
     return batched ? "__ldg(mv + " + std::to_string(k) + ")" : "P.pres[" + std::to_string(k) + "].pre";
@@ -72,7 +72,7 @@ std::string jit_generate_turn(const LineParams& p, int L, int NL, int warps, boo
                    : "P.f[" + std::to_string(fi) + "].noise_base";
   };
   // block = (W, M, NL) threads
-  const bool split = turn_split_form(L);
+  const bool split = split_form && L >= 512;
   const int M = line_threads(L, 1, 1, split);   // LineCfg<L, split>::M
   const int threads = p.W > 0 ? p.W * M * NL : 256;
   const int min_blocks = std::max(1, warps * 32 / threads);

@@ -16,7 +16,9 @@ namespace cupssgb {
 // __launch_bounds__ minimum block count is warps * 32 / threads per block; with a
 // width-generic kernel, p.W = 0, blocks of 256 threads are assumed).
 // batched: numerical values come from the batch member's row of P.mvals.
-std::string jit_generate_turn(const LineParams& p, int L, int NL, int warps = 16, bool batched = false);
+// split: lines of 512 and 1024 points in the split FFT form (turn_split_form(L) is the
+// automatic choice).
+std::string jit_generate_turn(const LineParams& p, int L, int NL, int warps, bool batched, bool split);
 // Compiles (once per source text) and returns the kernel handle.  Throws Error.
 cudaKernel_t jit_kernel(const std::string& source, const char* entry);
 // Compiles for sm_103a without loading (no GPU needed); returns "" or the log.

@@ -68,6 +68,7 @@ int split_override();
 // CUPSSGB_PLANE_C sets want_c when it is 0), with *ps the plane-store pitch for nc input
 // columns and *smem the dynamic shared memory of one CTA.
 int plane_pass_shape(int Lx, int sy, int nc, int* ps, size_t* smem, int want_c = 0);
+int plane_cluster_override();   // CUPSSGB_PLANE_C, or 0
 cudaError_t launch_plane_pass(const PlaneParams& p, int Lx, int sy, int sz, int nz, int c, cudaStream_t st,
                               bool pdl);
 

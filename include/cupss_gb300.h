@@ -188,6 +188,19 @@ int cupssgb_solver_get_real_member_device(cupssgb_solver* s, int field, int memb
 /* JSON {"phaseN": {"W": chosen, "ms": {candidate: ms per phase}}}; same buffer rules
  * as kernel_report. */
 int cupssgb_solver_tune_report(cupssgb_solver* s, char* buf, int buflen);
+/* Autotuner cache.  prepare times the launch shapes of each phase (turnaround tile
+ * width, its resident-warp target, the FFT form of 512/1024-point lines, CTAs per plane
+ * of the 3D xy-plane pass) and stores the winners in a text file keyed by GPU, grid,
+ * batch span and update program; a later prepare with the same key reads them instead
+ * of timing.  File: $CUPSSGB_TUNE_CACHE ("" or "off": no cache), else
+ * $XDG_CACHE_HOME/cupss_gb300/tune_v1.txt, else $HOME/.cache/cupss_gb300/tune_v1.txt;
+ * lines "cupssgb-tune-v1<TAB>key<TAB>value", appended, the last line of a key wins.
+ * CUPSSGB_TUNE=0 turns tuning off.  These three calls expose the file for tools and
+ * tests: the path ("" when off), the value of a key (returns its length, or
+ * CUPSSGB_ERR_INVALID when absent), and appending an entry. */
+int cupssgb_tune_cache_path(char* buf, int buflen);
+int cupssgb_tune_cache_lookup(const char* key, char* value, int buflen);
+int cupssgb_tune_cache_store(const char* key, const char* value);
 /* Device bytes prepare would allocate for a batch of `members` (no GPU needed). */
 long long cupssgb_solver_estimate_bytes(cupssgb_solver* s, int members);
 /* 1 when all work queued on the solver's stream has finished, 0 while it runs. */

@@ -56,7 +56,7 @@ def kernels_run(e, steps):
 def test_plane_pass_equals_row_pass_form(shape, monkeypatch):
     sx, sy, sz = shape
     init = np.random.default_rng(sx + sz).uniform(-0.05, 0.05, sx * sy * sz).astype(np.float32)
-    monkeypatch.delenv("CUPSSGB_PLANE", raising=False)
+    monkeypatch.setenv("CUPSSGB_PLANE", "1")
     a = make(shape, init)
     ka = kernels_run(a, 3)
     a.advanceTime(37)
@@ -75,8 +75,9 @@ def test_plane_pass_equals_row_pass_form(shape, monkeypatch):
     assert err < 1e-6
 
 
-def test_plane_pass_in_a_batch_equals_single_solves():
+def test_plane_pass_in_a_batch_equals_single_solves(monkeypatch):
     import cupss_gb300 as c
+    monkeypatch.setenv("CUPSSGB_PLANE", "1")
     from cupss_gb300.workloads import SYSTEMS, declare
     shape = (32, 32, 32)
     ens = c.Ensemble()

@@ -8,6 +8,7 @@
 #include <map>
 #include <sstream>
 
+#include "fft.cuh"
 #include "jit.h"
 #include "launch.h"
 
@@ -204,16 +205,10 @@ void Solver::prepare() {
   const size_t half = half_;
   const size_t hall = half_ * (size_t)nmem_;   // all members
   const int F = nfields();
-  // twiddle super-table: table for length L at offset L, L = 1..2048
+  // twiddle super-table (fft.cuh: tw_base): lengths 2^a up to 2048 and 3 * 2^a up to 1536
   {
-    const int Lmax = 2048;
-    std::vector<float2> h(2 * Lmax);
-    h[0] = make_float2(0.f, 0.f);
-    for (int L = 1; L <= Lmax; L *= 2)
-      for (int j = 0; j < L; ++j) {
-        const double a = -2.0 * M_PI * (double)j / (double)L;
-        h[L + j] = make_float2((float)std::cos(a), (float)std::sin(a));
-      }
+    std::vector<float2> h(kTwLen);
+    fill_twiddle_table(h.data());
     tw_ = (float2*)dalloc(h.size() * sizeof(float2));
     check(cudaMemcpyAsync(tw_, h.data(), h.size() * sizeof(float2), cudaMemcpyHostToDevice, stream_),
           "twiddle upload");

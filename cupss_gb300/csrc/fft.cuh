@@ -1,10 +1,11 @@
 // Register/shared-memory FFT building blocks for the GB300 pseudospectral engine.
 //
-// A line of length L (power of two, 1..1024) is split as L = R * M: M threads cooperate
-// on one line and each holds R complex values in registers.  The four-step form uses
-// M = 2^floor(log2(L)/2) (R is M or 2M).  Lines of 512 and 1024 points can instead take
-// the split form below (template flag SP): R = 16 and M = L/16 threads, so that a pass
-// over few long lines (a 2D grid) still gives the GPU enough threads.
+// A line of length L (a power of two 1..1024, or 3 * 2^a up to 384) is split as
+// L = R * M: M threads cooperate on one line and each holds R complex values in
+// registers.  The four-step form uses M = 2^floor(a/2) for L = 2^a or 3 * 2^a (R is M or
+// 2M, or 3M or 6M).  Lines of 512 and 1024 points can instead take the split form below
+// (template flag SP): R = 16 and M = L/16 threads, so that a pass over few long lines (a
+// 2D grid) still gives the GPU enough threads.
 //
 //   step-1 layout: thread m holds positions  n = m + M*r,            r in [0,R)
 //   step-2 layout: thread m holds positions  k = s + R*k',  s = m + M*j,
@@ -19,7 +20,8 @@
 //
 // The four-step split X[s + R k'] = sum_m W_M^{m k'} W_L^{m s} sum_r x[m + M r] W_R^{r s}
 // is the standard Cooley-Tukey factorisation; the register DFTs are recursive
-// radix-2 decimation in time with compile-time twiddles.
+// radix-2 decimation in time with compile-time twiddles, ending in a radix-3 butterfly
+// for orders 3 * 2^b.
 //
 // Split form (M = G*R threads, G = 2 or 4): the radix-M DFT of step 2 is itself split
 // with m = a + R b, k' = e + G f (a, f in [0,R); b, e in [0,G)):
@@ -110,10 +112,12 @@ CG_HD float2 c_scale(float2 a, float s) { return make_float2(a.x * s, a.y * s); 
 CG_HD float2 c_muli(float2 a) { return make_float2(-a.y, a.x); }    // i * a
 CG_HD float2 c_mulmi(float2 a) { return make_float2(a.y, -a.x); }   // -i * a
 
-// Multiply by W_N^K (forward, W = exp(-2 pi i/N)) or its conjugate (INV), N <= 64.
+// Multiply by W_N^K (forward, W = exp(-2 pi i/N)) or its conjugate (INV), N dividing 64
+// or 192.
 template <int N, int K, bool INV>
 CG_HD float2 tw_const(float2 a) {
   constexpr int k = K % N;
+  static_assert(64 % N == 0 || 192 % N == 0, "compile-time twiddles of orders dividing 64 or 192");
   if constexpr (k == 0) {
     return a;
   } else if constexpr (4 * k == N) {
@@ -122,13 +126,21 @@ CG_HD float2 tw_const(float2 a) {
     return make_float2(-a.x, -a.y);
   } else if constexpr (4 * k == 3 * N) {
     return INV ? c_mulmi(a) : c_muli(a);
-  } else {
+  } else if constexpr (64 % N == 0) {
     constexpr int j = k * (64 / N);
     constexpr float wr = kTw64Re[j];
     constexpr float wi = INV ? -kTw64Im[j] : kTw64Im[j];
     return c_mul(a, make_float2(wr, wi));
+  } else {
+    constexpr int j = k * (192 / N);
+    constexpr float wr = kTw192Re[j];
+    constexpr float wi = INV ? -kTw192Im[j] : kTw192Im[j];
+    return c_mul(a, make_float2(wr, wi));
   }
 }
+
+// sqrt(3)/2 rounded to float (the imaginary part of W_3 = exp(-2 pi i/3))
+constexpr float kSqrt3Half = 0x1.bb67aep-1f;
 
 // In-place DFT of the N values v[O + S*i], i in [0,N), natural-order output.
 template <int N, bool INV, int S>
@@ -173,6 +185,17 @@ struct Dft {
       float2 a = v[O], b = v[O + S];
       v[O] = p_add(a, b);
       v[O + S] = p_sub(a, b);
+    } else if constexpr (N == 3) {
+      // X0 = a + (b + c), X1,2 = a - (b + c)/2 -+ i sqrt(3)/2 (b - c) (forward; + for INV)
+      const float2 a = v[O], b = v[O + S], c = v[O + 2 * S];
+      const float2 t = p_add(b, c);
+      const float2 u = make_float2(a.x - 0.5f * t.x, a.y - 0.5f * t.y);
+      const float2 d = p_sub(b, c);
+      const float2 w = INV ? make_float2(-kSqrt3Half * d.y, kSqrt3Half * d.x)
+                           : make_float2(kSqrt3Half * d.y, -kSqrt3Half * d.x);
+      v[O] = p_add(a, t);
+      v[O + S] = p_add(u, w);
+      v[O + 2 * S] = p_sub(u, w);
     } else {
       Dft<N / 2, INV, 2 * S>::template run<O>(v);
       Dft<N / 2, INV, 2 * S>::template run<O + S>(v);
@@ -181,40 +204,69 @@ struct Dft {
   }
 };
 
+// log2 of the power-of-two part of a supported line length (L = 2^a or 3 * 2^a), -1 else
+CG_HD constexpr int line_log2(int L) {
+  int n = (L % 3 == 0) ? L / 3 : L;
+  int a = 0;
+  while (n > 1 && n % 2 == 0) {
+    n /= 2;
+    ++a;
+  }
+  return n == 1 ? a : -1;
+}
+CG_HD constexpr bool line_pow2(int L) { return L >= 1 && (L & (L - 1)) == 0; }
+
 template <int L, bool SP = false>
 struct LineCfg {
-  static constexpr int lg = (L <= 1) ? 0 : (L == 2 ? 1 : (L == 4 ? 2 : (L == 8 ? 3 : (L == 16 ? 4 :
-                            (L == 32 ? 5 : (L == 64 ? 6 : (L == 128 ? 7 : (L == 256 ? 8 :
-                            (L == 512 ? 9 : (L == 1024 ? 10 : -1))))))))));
-  static_assert(lg >= 0, "line length must be a power of two in [1, 1024]");
-  static constexpr bool kSplit = SP && (L >= 512);
+  static constexpr int lg = line_log2(L);
+  static_assert(lg >= 0 && (line_pow2(L) ? L <= 1024 : L <= 384),
+                "line length must be 2^a in [1, 1024] or 3 * 2^a up to 384");
+  static constexpr bool kSplit = SP && (L >= 512) && line_pow2(L);
   static constexpr int M = kSplit ? L / 16 : (1 << (lg / 2));   // threads per line
   static constexpr int R = L / M;                               // values per thread
-  static constexpr int J = kSplit ? 1 : R / M;   // s-values per thread in step 2 (1 or 2)
+  static constexpr int J = kSplit ? 1 : R / M;   // s-values per thread in step 2 (1, 2, 3 or 6)
   static constexpr int G = kSplit ? M / R : 1;   // split form: threads per s-value in step 2
 };
 
 // Host-side threads per line (equals LineCfg<L, split>::M for every supported L).
 CG_HD int line_m_of(int L, bool split) {
-  if (split && L >= 512) return L / 16;
-  int lg = 0;
-  while ((1 << lg) < L) ++lg;
-  return 1 << (lg / 2);
+  if (split && L >= 512 && line_pow2(L)) return L / 16;
+  return 1 << (line_log2(L) / 2);
 }
 
-// Twiddle super-table: the table for length L lives at tw + L and holds
-// exp(-2 pi i j / L) for j in [0, L).
+// Twiddle super-table: the table for length L holds exp(-2 pi i j / L) for j in [0, L)
+// and starts at tw + L for powers of two (L <= 2048) and at tw + kTwOdd + L for lengths
+// 3 * 2^a (L <= 1536).
 // The device load is a volatile read-only load: a kernel that runs a forward and an
 // inverse transform of the same length reads the same twiddles twice, and letting the
 // compiler merge those loads keeps every twiddle live in registers between the two
 // transforms (spills and lower occupancy); an L1 hit is cheaper than that.
+constexpr int kTwOdd = 4096;
+constexpr int kTwLen = kTwOdd + 2 * 1536;   // float2 entries of the whole table
+CG_HD int tw_base(int L) { return line_pow2(L) ? L : kTwOdd + L; }
+#if !defined(__CUDACC_RTC__)
+// Host: fills the kTwLen entries (double-precision angles rounded once to float).
+inline void fill_twiddle_table(float2* h) {
+  for (int i = 0; i < kTwLen; ++i) h[i] = make_float2(0.f, 0.f);
+  for (int L = 1; L <= 2048; L *= 2)
+    for (int j = 0; j < L; ++j) {
+      const double a = -2.0 * 3.14159265358979323846 * (double)j / (double)L;
+      h[tw_base(L) + j] = make_float2((float)__builtin_cos(a), (float)__builtin_sin(a));
+    }
+  for (int L = 3; L <= 1536; L *= 2)
+    for (int j = 0; j < L; ++j) {
+      const double a = -2.0 * 3.14159265358979323846 * (double)j / (double)L;
+      h[tw_base(L) + j] = make_float2((float)__builtin_cos(a), (float)__builtin_sin(a));
+    }
+}
+#endif
 CG_HD float2 tw_load(const float2* tw, int L, int j) {
 #if defined(__CUDA_ARCH__)
   float2 w;
-  asm volatile("ld.global.nc.v2.f32 {%0, %1}, [%2];" : "=f"(w.x), "=f"(w.y) : "l"(tw + L + j));
+  asm volatile("ld.global.nc.v2.f32 {%0, %1}, [%2];" : "=f"(w.x), "=f"(w.y) : "l"(tw + tw_base(L) + j));
   return w;
 #else
-  return tw[L + j];
+  return tw[tw_base(L) + j];
 #endif
 }
 
@@ -234,21 +286,19 @@ CG_HD void fwd_step1(float2 (&v)[LineCfg<L, SP>::R], int m, const float2* tw) {
 
 // Step-2 DFTs of the four-step form: register index j*M + k holds position s*M + k
 // (s = m + M j) of the transposed data; output register j*M + k' holds X[s + R k'].
+template <int L, bool SP, bool INV, int... Js>
+CG_HD void dft2_each(float2* v, iseq<Js...>) {
+  (Dft<LineCfg<L, SP>::M, INV, 1>::template run<Js * LineCfg<L, SP>::M>(v), ...);
+}
 template <int L, bool SP = false>
 CG_HD void fwd_dft2(float2 (&v)[LineCfg<L, SP>::R]) {
-  constexpr int M = LineCfg<L, SP>::M;
-  constexpr int J = LineCfg<L, SP>::J;
-  if constexpr (J >= 1) Dft<M, false, 1>::template run<0>(v);
-  if constexpr (J >= 2) Dft<M, false, 1>::template run<M>(v);
+  dft2_each<L, SP, false>(v, make_iseq<LineCfg<L, SP>::J>{});
 }
 // register j*M + k' holds X[s + R k']; out register j*M + m' holds
 // y_{m'}[s] = sum_k' X[s + R k'] W_M^{-m' k'}  (to be stored at position s*M + m').
 template <int L, bool SP = false>
 CG_HD void inv_dft2(float2 (&v)[LineCfg<L, SP>::R]) {
-  constexpr int M = LineCfg<L, SP>::M;
-  constexpr int J = LineCfg<L, SP>::J;
-  if constexpr (J >= 1) Dft<M, true, 1>::template run<0>(v);
-  if constexpr (J >= 2) Dft<M, true, 1>::template run<M>(v);
+  dft2_each<L, SP, true>(v, make_iseq<LineCfg<L, SP>::J>{});
 }
 
 // W_G^q = exp(-2 pi i q / G) for G = 2 or 4: one of +-1, +-i, exact.
@@ -361,6 +411,9 @@ CG_HD void inv_load_step1(float2 (&v)[LineCfg<L, SP>::R], int m, const float2* t
   }
   inv_step1<L, SP>(v, m, tw);
 }
+
+// Index of the partner -k of k (mod n), k in [0, n).
+CG_HD int neg_mod(int k, int n) { return k == 0 ? 0 : n - k; }
 
 // Position of register index idx in the step-1 / step-2 layouts.  Both are cyclic:
 // pos = m + step2_off(idx) with the offset a multiple of M.

@@ -53,8 +53,8 @@ __global__ void expand_spectrum(const ExpandParams p) {
     const int kx = (int)(idx % p.sx);
     const int ky = (int)((idx / p.sx) % p.sy);
     const int kz = (int)(idx / ((size_t)p.sx * p.sy));
-    const int pky = (p.sy - ky) & (p.sy - 1);
-    const int pkz = (p.sz - kz) & (p.sz - 1);
+    const int pky = neg_mod(ky, p.sy);
+    const int pkz = neg_mod(kz, p.sz);
     float2 out;
     if (kx > 0 && 2 * kx < p.sx) {
       out = p.spec[((size_t)kz * p.sy + ky) * p.Lx + kx];
@@ -76,8 +76,8 @@ __global__ void compress_spectrum(const CompressParams p) {
     const int kx = (int)(idx % p.Lx);
     const int ky = (int)((idx / p.Lx) % p.sy);
     const int kz = (int)(idx / ((size_t)p.Lx * p.sy));
-    const int pky = (p.sy - ky) & (p.sy - 1);
-    const int pkz = (p.sz - kz) & (p.sz - 1);
+    const int pky = neg_mod(ky, p.sy);
+    const int pkz = neg_mod(kz, p.sz);
     const size_t row = ((size_t)kz * p.sy + ky) * p.sx, prow = ((size_t)pkz * p.sy + pky) * p.sx;
     float2 out;
     if (kx > 0) {
@@ -106,8 +106,8 @@ __global__ void mask_spectrum(const MaskParams p) {
     if (kx > 0) {
       if (kyz && keep(kx, p.sx, p.xlim)) out = c_scale(p.spec[idx], p.scale);
     } else {
-      const int pky = (p.sy - ky) & (p.sy - 1);
-      const int pkz = (p.sz - kz) & (p.sz - 1);
+      const int pky = neg_mod(ky, p.sy);
+      const int pkz = neg_mod(kz, p.sz);
       const float2 z = p.spec[idx];
       const float2 zp = p.spec[((size_t)pkz * p.sy + pky) * p.Lx];
       const float2 c0 = unpack(z, zp, 0), cn = unpack(z, zp, 1);

@@ -80,7 +80,8 @@ __device__ __forceinline__ void static_for(iseq<I...>, F&& f) {
 // per register; usable while 2R <= 64 (the compile-time twiddle table).
 template <int LX, bool SP>
 struct RowTwSplit {
-  static constexpr bool value = (2 * LineCfg<LX, SP>::R <= 64) && (LineCfg<LX, SP>::M > 1);
+  static constexpr int N = 2 * LineCfg<LX, SP>::R;
+  static constexpr bool value = (64 % N == 0 || 192 % N == 0) && (LineCfg<LX, SP>::M > 1);
 };
 template <int LX, bool SP, int I>
 __device__ __forceinline__ float2 row_twiddle(float2 wm) {
@@ -98,13 +99,13 @@ __device__ __forceinline__ void row_c2r(float2 (&v)[LineCfg<LX, SP>::R], const f
     static_for(make_iseq<R>{}, [&](auto I) {
       constexpr int i = decltype(I)::value;
       const int k = pos_step2<LX, SP>(m, i);
-      v[i] = c2r_pre_w(v[i], T[pad_pos<LX, SP>((LX - k) & (LX - 1))], k, row_twiddle<LX, SP, i>(wm));
+      v[i] = c2r_pre_w(v[i], T[pad_pos<LX, SP>(neg_mod(k, LX))], k, row_twiddle<LX, SP, i>(wm));
     });
   } else {
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       const int k = pos_step2<LX, SP>(m, i);
-      v[i] = c2r_pre(v[i], T[pad_pos<LX, SP>((LX - k) & (LX - 1))], k, sx, tw);
+      v[i] = c2r_pre(v[i], T[pad_pos<LX, SP>(neg_mod(k, LX))], k, sx, tw);
     }
   }
 }
@@ -120,14 +121,14 @@ __device__ __forceinline__ void row_r2c_store(const float2 (&v)[LineCfg<LX, SP>:
     static_for(make_iseq<R>{}, [&](auto I) {
       constexpr int i = decltype(I)::value;
       const int k = pos_step2<LX, SP>(m, i);
-      const float2 x = r2c_post_w(v[i], T[pad_pos<LX, SP>((LX - k) & (LX - 1))], k, row_twiddle<LX, SP, i>(wm));
+      const float2 x = r2c_post_w(v[i], T[pad_pos<LX, SP>(neg_mod(k, LX))], k, row_twiddle<LX, SP, i>(wm));
       if (live) out[k] = x;
     });
   } else {
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       const int k = pos_step2<LX, SP>(m, i);
-      const float2 x = r2c_post(v[i], T[pad_pos<LX, SP>((LX - k) & (LX - 1))], k, sx, tw);
+      const float2 x = r2c_post(v[i], T[pad_pos<LX, SP>(neg_mod(k, LX))], k, sx, tw);
       if (live) out[k] = x;
     }
   }

@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(512, 1) plane_pass(const PlaneParams p) {
       static_for(make_iseq<RXV>{}, [&](auto I) {
         constexpr int i = decltype(I)::value;
         const int k = pos_step2<LX>(m, i);
-        const int km = (LX - k) & (LX - 1);
+        const int km = neg_mod(k, LX);
         const float2 mir = km < p.nc ? row[km] : make_float2(0.f, 0.f);
         if constexpr (RowTwSplit<LX, false>::value) {
           v[i] = c2r_pre_w(v[i], mir, k, row_twiddle<LX, false, i>(wm));
@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(512, 1) plane_pass(const PlaneParams p) {
         constexpr int i = decltype(I)::value;
         constexpr int own = step2_off<LX>(i) / CX;
         const int k = pos_step2<LX>(m, i);
-        const float2 zm = TB[pad_pos<LX>((LX - k) & (LX - 1))];
+        const float2 zm = TB[pad_pos<LX>(neg_mod(k, LX))];
         float2 x;
         if constexpr (RowTwSplit<LX, false>::value) {
           x = r2c_post_w(v[i], zm, k, row_twiddle<LX, false, i>(wm));

@@ -168,8 +168,8 @@ __device__ __forceinline__ float2 noise_at(const LineParams& P, const Dims& d, c
     return upper ? hi : lo;
   }
   const uint32_t lin = ((uint32_t)kz * d.sy + ky) * d.sx + kx;
-  const int pky = (d.sy - ky) & (d.sy - 1);
-  const int pkz = (d.sz - kz) & (d.sz - 1);
+  const int pky = neg_mod(ky, d.sy);
+  const int pkz = neg_mod(kz, d.sz);
   const uint32_t plin = ((uint32_t)pkz * d.sy + pky) * d.sx + kx;
   uint32_t ctr = lin;
   bool conj = false;

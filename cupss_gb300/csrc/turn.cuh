@@ -323,7 +323,7 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
         const int pos = pos_step2<L, SP>(m, i);
         const int ky = Z3 ? g.lineky : pos;
         const int kz = Z3 ? pos : 0;
-        const int ppos = (L - pos) & (L - 1);
+        const int ppos = neg_mod(pos, L);
         Fetch fx;
         fx.smem = smem;
         fx.slot_sz = slot_sz;

@@ -12,14 +12,8 @@
 using namespace cupssgb;
 
 static std::vector<float2> make_twiddles() {
-  const int Lmax = 2048;
-  std::vector<float2> h(2 * Lmax);
-  h[0] = make_float2(0.f, 0.f);
-  for (int L = 1; L <= Lmax; L *= 2)
-    for (int j = 0; j < L; ++j) {
-      const double a = -2.0 * M_PI * (double)j / (double)L;
-      h[L + j] = make_float2((float)std::cos(a), (float)std::sin(a));
-    }
+  std::vector<float2> h(kTwLen);
+  fill_twiddle_table(h.data());
   return h;
 }
 
@@ -125,8 +119,20 @@ int main() {
   bad += check<256, true>(tw, 12);
   bad += check<512, true>(tw, 13);
   bad += check<1024, true>(tw, 14);
+  // lengths 3 * 2^a: radix-3 butterflies in the register DFTs, J = R/M of 3 or 6
+  bad += check<3, false>(tw, 15);
+  bad += check<6, false>(tw, 16);
+  bad += check<12, false>(tw, 17);
+  bad += check<24, false>(tw, 18);
+  bad += check<48, false>(tw, 19);
+  bad += check<96, false>(tw, 20);
+  bad += check<192, false>(tw, 21);
+  bad += check<384, false>(tw, 22);
   for (int L = 1; L <= 1024; L *= 2)
     if (line_m_of(L, false) <= 0 || line_m_of(L, true) <= 0) bad++;
+  if (line_m_of(96, false) != LineCfg<96>::M || line_m_of(192, true) != LineCfg<192, true>::M ||
+      line_m_of(384, false) != LineCfg<384>::M || line_m_of(3, false) != LineCfg<3>::M)
+    bad++;
   if (line_m_of(512, true) != LineCfg<512, true>::M || line_m_of(1024, true) != LineCfg<1024, true>::M ||
       line_m_of(1024, false) != LineCfg<1024>::M || line_m_of(64, true) != LineCfg<64>::M)
     bad++;

@@ -512,8 +512,8 @@ def bench_served(args):
     line = {"metric": "served solves/s", "value": len(reqs) / makespan, "unit": "solves/s", "n_gpus": 1,
             "steps": None, "warmup": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic Poisson stream, seed 20261203",
-            "config": {"workload": "served: %d requests, Poisson rate %.2f/s, {EW, KPZ, CH} 2D 64^2..1024^2, "
-                                   "CH 3D 64^3..128^3, steps log-U[1e3,1e5]" % (len(reqs), args.rate),
+            "config": {"workload": "served: %d requests, Poisson rate %.2f/s, {EW, KPZ, CH} 2D 64^2..1024^2 (incl. 96^2, 192^2), "
+                                   "CH 3D 64^3..192^3, steps log-U[1e3,1e5]" % (len(reqs), args.rate),
                        "requests": len(reqs), "rate_per_s": args.rate, "hbm_budget": args.hbm_budget,
                        "max_slots": args.max_slots, "max_chunk": args.max_chunk, "pool_keys": len(keys),
                        "total_pt_steps": work},

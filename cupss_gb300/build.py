@@ -19,7 +19,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcupss.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = [
-    "k_line_1024.cu", "k_line_512.cu", "k_line_256.cu", "k_line_128.cu", "k_line_small.cu",
+    "k_line_1024.cu", "k_line_512.cu", "k_line_256.cu", "k_line_128.cu", "k_line_small.cu", "k_line_r3.cu",
     "k_row.cu", "k_plane.cu", "k_misc.cu", "noalloc.cu",
     "engine.cpp", "engine_batch.cpp", "capi.cpp", "jit.cpp",
     "host_parser.cpp", "host_evolver.cpp", "host_field_term.cpp", "host_init.cpp", "host_utils.cpp",

@@ -18,6 +18,10 @@ namespace {
 constexpr float kPiF = 3.1415926535f;   // the reference's PI (inc/cupss/defines.h:57)
 
 bool pow2(int n) { return n >= 1 && (n & (n - 1)) == 0; }
+// 3 * 2^a with a >= 1 (even, so that Nyquist bins and Hermitian line pairs exist)
+bool three_pow2(int n) { return n >= 6 && n % 3 == 0 && pow2(n / 3) && n % 2 == 0; }
+// supported axis lengths: 2^a up to pow2_max, 3 * 2^a up to odd_max
+bool axis_ok(int n, int pow2_max, int odd_max) { return (pow2(n) && n <= pow2_max) || (three_pow2(n) && n <= odd_max); }
 
 std::string cuda_msg(cudaError_t e, const char* what) {
   std::ostringstream os;
@@ -35,9 +39,10 @@ Solver::Solver(int sx, int sy, int sz, float dx, float dy, float dz, float dt)
   if (const char* b = std::getenv("CUPSSGB_TURN_WARPS")) turn_warps_ = std::max(1, std::atoi(b));
   if (const char* d = std::getenv("CUPSSGB_PDL")) pdl_ = std::string(d) != "0";
   if (const char* d = std::getenv("CUPSSGB_PLANE")) plane_env_ = std::string(d) == "0" ? 0 : 1;
-  if (!pow2(sx) || sx < 2 || sx > 2048 || !pow2(sy) || sy > 1024 || !pow2(sz) || sz > 1024)
+  if (sx < 2 || !axis_ok(sx, 2048, 384) || !axis_ok(sy, 1024, 192) || !axis_ok(sz, 1024, 192))
     throw Error(kErrUnsupported,
-                "grid sizes must be powers of two: 2 <= sx <= 2048, 1 <= sy, sz <= 1024");
+                "grid sizes must be 2^a or 3*2^a: sx in [2, 2048] (3*2^a up to 384), sy and sz in [1, 1024] "
+                "(3*2^a up to 192)");
   // dimension rule of the reference (src/evolver.cpp:22-36)
   dim_ = (sz == 1 && sy == 1) ? 1 : (sz == 1 ? 2 : 3);
   Lx_ = sx / 2;

@@ -7,7 +7,8 @@ namespace cupssgb {
 
 static_assert(LineCfg<1>::M == 1 && LineCfg<8>::M == 2 && LineCfg<16>::M == 4 && LineCfg<256>::M == 16 &&
                   LineCfg<512>::M == 16 && LineCfg<1024>::M == 32 && LineCfg<256, true>::M == 16 &&
-                  LineCfg<512, true>::M == 32 && LineCfg<1024, true>::M == 64,
+                  LineCfg<512, true>::M == 32 && LineCfg<1024, true>::M == 64 && LineCfg<96>::M == 4 &&
+                  LineCfg<192>::M == 8 && LineCfg<6>::M == 1,
               "line_m_of must follow LineCfg");
 static int pl_of(int L, bool split) { return L + L / line_m_of(L, split); }
 
@@ -42,6 +43,12 @@ cudaError_t launch_line_pass(const LineParams& p, int nl, int nslots, dim3 grid,
     case 256: return launch_line_256(p, nl, smem, grid, st, pdl);
     case 512: return launch_line_512(p, nl, smem, grid, st, pdl);
     case 1024: return launch_line_1024(p, nl, smem, grid, st, pdl);
+    case 6: return launch_line_6(p, nl, smem, grid, st, pdl);
+    case 12: return launch_line_12(p, nl, smem, grid, st, pdl);
+    case 24: return launch_line_24(p, nl, smem, grid, st, pdl);
+    case 48: return launch_line_48(p, nl, smem, grid, st, pdl);
+    case 96: return launch_line_96(p, nl, smem, grid, st, pdl);
+    case 192: return launch_line_192(p, nl, smem, grid, st, pdl);
     default: return cudaErrorInvalidValue;
   }
 }

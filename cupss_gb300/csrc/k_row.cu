@@ -1,4 +1,4 @@
-// Row-pass instantiations and dispatch by Lx = sx/2.
+// Row-pass instantiations and dispatch by Lx = sx/2 (2^a up to 1024, 3 * 2^a up to 192).
 #include "kernels.cuh"
 #include "launch.h"
 
@@ -67,6 +67,14 @@ cudaError_t launch_row_pass(const XParams& p, cudaStream_t st, int nz, bool pdl)
     case 256: return launch_row_t<256>(p, st, nz, pdl);
     case 512: return launch_row_t<512>(p, st, nz, pdl);
     case 1024: return launch_row_t<1024>(p, st, nz, pdl);
+    // rows of 3 * 2^a packed points (sx = 6 .. 384)
+    case 3: return launch_row_t<3>(p, st, nz, pdl);
+    case 6: return launch_row_t<6>(p, st, nz, pdl);
+    case 12: return launch_row_t<12>(p, st, nz, pdl);
+    case 24: return launch_row_t<24>(p, st, nz, pdl);
+    case 48: return launch_row_t<48>(p, st, nz, pdl);
+    case 96: return launch_row_t<96>(p, st, nz, pdl);
+    case 192: return launch_row_t<192>(p, st, nz, pdl);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -84,6 +84,8 @@ cudaError_t launch_tick(MemberK* members, int n, uint32_t inc, cudaStream_t st, 
 CUPSSGB_DECL_LINE(1) CUPSSGB_DECL_LINE(2) CUPSSGB_DECL_LINE(4) CUPSSGB_DECL_LINE(8)
 CUPSSGB_DECL_LINE(16) CUPSSGB_DECL_LINE(32) CUPSSGB_DECL_LINE(64) CUPSSGB_DECL_LINE(128)
 CUPSSGB_DECL_LINE(256) CUPSSGB_DECL_LINE(512) CUPSSGB_DECL_LINE(1024)
+CUPSSGB_DECL_LINE(6) CUPSSGB_DECL_LINE(12) CUPSSGB_DECL_LINE(24) CUPSSGB_DECL_LINE(48)
+CUPSSGB_DECL_LINE(96) CUPSSGB_DECL_LINE(192)
 #undef CUPSSGB_DECL_LINE
 
 }  // namespace cupssgb

@@ -66,8 +66,8 @@ def kpz_ensemble(n=512, seed=DEFAULT_SEED, sizes=(64, 128, 256, 512)):
 
 def served_stream(n=64, rate=2.0, seed=DEFAULT_SEED):
     """Poisson stream of solve requests drawn uniformly from {2D Edwards-Wilkinson, 2D
-    KPZ, 2D Cahn-Hilliard, 3D Cahn-Hilliard}: 2D sides uniform over {64..1024} (log-
-    uniform in N), 3D sides over {64, 128} (the powers of two in 64..192), step counts
+    KPZ, 2D Cahn-Hilliard, 3D Cahn-Hilliard}: 2D sides uniform over {64, 96, 128, 192, 256,
+    512, 1024}, 3D sides over {64, 96, 128, 192} (the sizes 2^a and 3 * 2^a in 64..192), step counts
     log-uniform in [1e3, 1e5], seeded parameters (nu ~ U[0.5, 2], KPZ lambda ~ U[0, 1],
     CH T ~ U[0, 0.01]) and seeded initial fields (CH: U[-0.1, 0.1]; EW, KPZ: flat).
     arrival: seconds after the first request."""
@@ -81,10 +81,10 @@ def served_stream(n=64, rate=2.0, seed=DEFAULT_SEED):
         kind = kinds[int(rng.integers(4))]
         steps = int(round(10.0 ** rng.uniform(3.0, 5.0)))
         if kind == "ch3d":
-            side = int(rng.choice([64, 128]))
+            side = int(rng.choice([64, 96, 128, 192]))
             shape = (side, side, side)
         else:
-            side = int(rng.choice([64, 128, 256, 512, 1024]))
+            side = int(rng.choice([64, 96, 128, 192, 256, 512, 1024]))
             shape = (side, side, 1)
         if kind == "ew":
             params, dt = {"nu": float(rng.uniform(0.5, 2.0))}, 0.01

@@ -424,7 +424,7 @@ def bench_ensemble(args):
                          "members_equal_to_plain": int(agree), "worst_rel_l2_vs_plain": worst,
                          "note": "members that diverge (large lambda^2 D / nu^3) do so identically in the plain "
                                  "solver: the semi-implicit scheme of the reference is unstable there"}}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def bench_served(args):
@@ -437,7 +437,8 @@ def bench_served(args):
     from cupss_gb300 import build as b
     from cupss_gb300.workloads import SYSTEMS, initial_fields, served_stream
     b.build()
-    reqs = served_stream(args.requests, args.rate)
+    steps_range = getattr(args, "steps_range", (1e3, 1e5))
+    reqs = served_stream(args.requests, args.rate, steps_range=steps_range)
     keys = sorted({(r["system"], r["shape"], r["dt"]) for r in reqs})
     srv = c.Server(hbm_budget=args.hbm_budget, max_slots=args.max_slots, max_chunk=args.max_chunk)
     sids = {k: srv.addSystem(SYSTEMS[k]) for k in ("ew", "kpz", "ch")}
@@ -513,7 +514,7 @@ def bench_served(args):
             "steps": None, "warmup": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic Poisson stream, seed 20261203",
             "config": {"workload": "served: %d requests, Poisson rate %.2f/s, {EW, KPZ, CH} 2D 64^2..1024^2 (incl. 96^2, 192^2), "
-                                   "CH 3D 64^3..192^3, steps log-U[1e3,1e5]" % (len(reqs), args.rate),
+                                   "CH 3D 64^3..192^3, steps log-U[%g,%g]" % (len(reqs), args.rate, *steps_range),
                        "requests": len(reqs), "rate_per_s": args.rate, "hbm_budget": args.hbm_budget,
                        "max_slots": args.max_slots, "max_chunk": args.max_chunk, "pool_keys": len(keys),
                        "total_pt_steps": work},
@@ -533,7 +534,7 @@ def bench_served(args):
     order = np.argsort([t[2] for t in times])[::-1][:6]
     line["last_finished"] = [[reqs[i]["system"], list(reqs[i]["shape"]), int(reqs[i]["steps"]),
                               round(times[i][1] - times[i][0], 3), round(float(lat[i]), 3)] for i in order]
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def dist_env():
@@ -578,11 +579,14 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--profile-steps", type=int, default=100)
     ap.add_argument("--no-cufft-ref", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the reduced ensemble and served lines")
     args = ap.parse_args()
     if args.workload == "kpz-ensemble":
-        return bench_ensemble(args)
+        print(json.dumps(bench_ensemble(args)), flush=True)
+        return
     if args.workload == "served":
-        return bench_served(args)
+        print(json.dumps(bench_served(args)), flush=True)
+        return
     wl = WORKLOADS[args.workload]
     K = args.steps if args.steps is not None else wl["steps"]
     W = args.warmup if args.warmup is not None else wl["warmup"]
@@ -716,13 +720,34 @@ def main():
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         cpu = run_cpu_baseline(wl)
 
+    # the batched and served forms, reduced so that the default run stays short: 64 KPZ
+    # members for 200 steps against their plain solves, and 24 served requests of 1e2..1e4
+    # steps (a tenth of the full stream's) at 8 requests/s against the plain FIFO
+    extra = {}
+    if rank == 0 and ws == 1 and not args.no_extra:
+        for key, fn, over in (("ensemble_reduced", bench_ensemble,
+                               dict(members=64, steps=200, plain_members=None)),
+                              ("served_reduced", bench_served,
+                               dict(requests=24, rate=8.0, steps_range=(1e2, 1e4)))):
+            try:
+                sub = argparse.Namespace(**vars(args))
+                for k2, v2 in over.items():
+                    setattr(sub, k2, v2)
+                r = fn(sub)
+                extra[key] = {k2: r.get(k2) for k2 in ("metric", "value", "unit", "speedup_vs_plain", "latency_s",
+                                                        "plain_sequential", "accuracy", "config", "pt_steps_per_s",
+                                                        "gpu_launches", "seconds", "makespan_s")
+                              if k2 in r}
+            except Exception as ex:   # report why, keep the headline line
+                extra[key] = {"unavailable": repr(ex)[:300]}
+
     if rank == 0:
         line = {"metric": "grid-pt-steps/s", "value": value, "unit": "pt-steps/s", "n_gpus": ws, "steps": K,
                 "warmup": W, "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic: SplitMix64 seed 20261203 uniform initial "
                 "field, Fourier-space Philox noise seed 42", "config": cfg, "roofline": roof,
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
-                "cufft_reference_schedule": cufft_ref}
+                "cufft_reference_schedule": cufft_ref, **extra}
         print(json.dumps(line), flush=True)
     e.close()
     if ws > 1:

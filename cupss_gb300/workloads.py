@@ -64,11 +64,11 @@ def kpz_ensemble(n=512, seed=DEFAULT_SEED, sizes=(64, 128, 256, 512)):
             for i in range(n)]
 
 
-def served_stream(n=64, rate=2.0, seed=DEFAULT_SEED):
+def served_stream(n=64, rate=2.0, seed=DEFAULT_SEED, steps_range=(1e3, 1e5)):
     """Poisson stream of solve requests drawn uniformly from {2D Edwards-Wilkinson, 2D
     KPZ, 2D Cahn-Hilliard, 3D Cahn-Hilliard}: 2D sides uniform over {64, 96, 128, 192, 256,
     512, 1024}, 3D sides over {64, 96, 128, 192} (the sizes 2^a and 3 * 2^a in 64..192), step counts
-    log-uniform in [1e3, 1e5], seeded parameters (nu ~ U[0.5, 2], KPZ lambda ~ U[0, 1],
+    log-uniform in steps_range (default [1e3, 1e5]), seeded parameters (nu ~ U[0.5, 2], KPZ lambda ~ U[0, 1],
     CH T ~ U[0, 0.01]) and seeded initial fields (CH: U[-0.1, 0.1]; EW, KPZ: flat).
     arrival: seconds after the first request."""
     rng = np.random.default_rng(seed)
@@ -79,7 +79,7 @@ def served_stream(n=64, rate=2.0, seed=DEFAULT_SEED):
     out = []
     for i in range(n):
         kind = kinds[int(rng.integers(4))]
-        steps = int(round(10.0 ** rng.uniform(3.0, 5.0)))
+        steps = int(round(10.0 ** rng.uniform(np.log10(steps_range[0]), np.log10(steps_range[1]))))
         if kind == "ch3d":
             side = int(rng.choice([64, 96, 128, 192]))
             shape = (side, side, side)

@@ -235,7 +235,9 @@ int cupssgb_device_info(char* buf, int buflen);
  * capture.  All calls share the one array: calls that can run at the same time on the
  * GPU (different streams, threads or processes sharing a context) race and must be
  * serialised by the caller.  Nothing in the array has to be cleared between calls:
- * each call writes every element it later reads. */
+ * each call writes every element it later reads.  The per-device set-up is done once
+ * per process: a cudaDeviceReset after the first call on a device discards the twiddle
+ * table, and calls on that device after such a reset are not supported. */
 int cupssgb_real_to_fourier_noalloc(const float* real_dev, float* fourier_dev, int sx, int sy, int sz,
                                     void* stream);
 

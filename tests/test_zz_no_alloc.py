@@ -6,7 +6,8 @@ fixed device array inside the library instead.  The test drives it through the C
 with caller-owned device buffers and checks it against the existing entry point
 (cupssgb_solver_set_real + cupssgb_solver_get_fourier) on two calls in a row, with
 different fields, so that nothing left in the shared working array from the first call
-leaks into the second.
+leaks into the second, and against numpy's FFT.  The shapes reach the size limit
+(2048 x 1024 = 2^21 points: 1024-point rows and columns).
 """
 import ctypes
 
@@ -28,7 +29,7 @@ def reference_fourier(field, shape):
     return out
 
 
-@pytest.mark.parametrize("shape", [(64, 32, 16), (256, 128, 1), (128, 1, 1)])
+@pytest.mark.parametrize("shape", [(64, 32, 16), (256, 128, 1), (128, 1, 1), (2048, 1024, 1)])
 def test_noalloc_matches_solver_path(built_lib, shape):
     import torch
     from cupss_gb300 import capi
@@ -51,6 +52,10 @@ def test_noalloc_matches_solver_path(built_lib, shape):
         ref = reference_fourier(field, shape)
         err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
         assert err < 1e-6, err
+        # and against an FFT that shares no code with the library (double precision)
+        exact = np.fft.fftn(field.astype(np.float64).reshape(sz, sy, sx))
+        err2 = np.linalg.norm(got - exact) / np.linalg.norm(exact)
+        assert err2 < 1e-5, err2
         outs.append(got)
     assert not np.allclose(outs[0], outs[1])
 

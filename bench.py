@@ -722,13 +722,14 @@ def main():
 
     # the batched and served forms, reduced so that the default run stays short: 64 KPZ
     # members for 200 steps against their plain solves, and 24 served requests of 1e2..1e4
-    # steps (a tenth of the full stream's) at 8 requests/s against the plain FIFO
+    # steps (a hundredth of the full stream's) arriving at 64 requests/s, which saturates
+    # both arms, against the plain FIFO
     extra = {}
     if rank == 0 and ws == 1 and not args.no_extra:
         for key, fn, over in (("ensemble_reduced", bench_ensemble,
                                dict(members=64, steps=200, plain_members=None)),
                               ("served_reduced", bench_served,
-                               dict(requests=24, rate=8.0, steps_range=(1e2, 1e4)))):
+                               dict(requests=24, rate=64.0, steps_range=(1e2, 1e4)))):
             try:
                 sub = argparse.Namespace(**vars(args))
                 for k2, v2 in over.items():

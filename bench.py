@@ -344,27 +344,48 @@ def bench_ensemble(args):
     dt = 0.005
     pts = sum(m["side"] ** 2 for m in members)
 
-    t0 = time.perf_counter()
-    ens = c.Ensemble()
-    declare(ens, sysd)
-    for m in members:
-        ens.addMember(m["side"], m["side"], 1, dt=dt, seed=m["seed"], nu=m["nu"], lam=m["lam"])
-    ens.prepare()
-    prep_s = time.perf_counter() - t0
-    ens.advance(3)   # captures the step graphs
-    clocks = Clocks(0)
-    clocks.start()
-    l0 = ens.launch_count
-    t0 = time.perf_counter()
-    ens.advance(steps)
-    outs = [ens.getReal(i, "h") for i in range(n)]
-    t_ens = time.perf_counter() - t0
-    clk = clocks.stop()
-    launches = ens.launch_count - l0
+    def run(fuse, sample_clocks):
+        # fuse=False: every grid size stepped by its own graphs on its own stream
+        old = os.environ.get("CUPSSGB_FUSE")
+        if not fuse:
+            os.environ["CUPSSGB_FUSE"] = "0"
+        try:
+            t0 = time.perf_counter()
+            ens = c.Ensemble()
+            declare(ens, sysd)
+            for m in members:
+                ens.addMember(m["side"], m["side"], 1, dt=dt, seed=m["seed"], nu=m["nu"], lam=m["lam"])
+            ens.prepare()
+            prep = time.perf_counter() - t0
+        finally:
+            if old is None:
+                os.environ.pop("CUPSSGB_FUSE", None)
+            else:
+                os.environ["CUPSSGB_FUSE"] = old
+        ens.advance(3)   # captures the step graphs
+        clocks = Clocks(0) if sample_clocks else None
+        if clocks:
+            clocks.start()
+        l0 = ens.launch_count
+        t0 = time.perf_counter()
+        ens.advance(steps)
+        res = [ens.getReal(i, "h") for i in range(n)]
+        t = time.perf_counter() - t0
+        r = {"seconds": t, "prepare_seconds": prep, "launches": ens.launch_count - l0, "outs": res,
+             "describe": ens.describe(), "device_bytes": ens.device_bytes,
+             "clocks": clocks.stop() if clocks else None}
+        ens.close()
+        return r
+
+    fused = run(True, True)
+    grouped = run(False, False)
+    t_ens, prep_s, launches, outs = fused["seconds"], fused["prepare_seconds"], fused["launches"], fused["outs"]
+    clk, groups, dev_bytes = fused["clocks"], fused["describe"], fused["device_bytes"]
     finite = [bool(np.isfinite(o).all()) for o in outs]
-    groups = ens.describe()
-    dev_bytes = ens.device_bytes
-    ens.close()
+    # the fused and grouped forms run the same arithmetic per member
+    fg_worst = max((float(np.linalg.norm(a.astype(np.float64) - b) / max(np.linalg.norm(b), 1e-30))
+                    for a, b in zip(outs, grouped["outs"]) if np.isfinite(a).all() and np.isfinite(b).all()),
+                   default=0.0)
 
     # the same solves with the plain evolver, one after another
     nplain = n if args.plain_members is None else min(n, args.plain_members)
@@ -420,6 +441,11 @@ def bench_ensemble(args):
                                  "members_run": nplain, "pt_steps_per_s": pts_plain * steps / t_plain},
             "speedup_vs_plain": t_plain_all / t_ens, "seconds": t_ens, "prepare_seconds": prep_s,
             "gpu_launches": launches, "clocks": clk,
+            "fused": groups.get("fused") is not None,
+            "grouped": {"value": n / grouped["seconds"], "unit": "solves/s", "seconds": grouped["seconds"],
+                        "gpu_launches": grouped["launches"], "prepare_seconds": grouped["prepare_seconds"],
+                        "worst_rel_l2_vs_fused": fg_worst,
+                        "what": "the same ensemble with CUPSSGB_FUSE=0: each grid size's own graphs on its own stream"},
             "accuracy": {"finite_members": int(sum(finite)), "members_compared": nplain,
                          "members_equal_to_plain": int(agree), "worst_rel_l2_vs_plain": worst,
                          "note": "members that diverge (large lambda^2 D / nu^3) do so identically in the plain "

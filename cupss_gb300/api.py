@@ -361,6 +361,20 @@ class Evolver:
         return json.loads(buf.value.decode())
 
 
+def multi_generated_sources(solvers):
+    """Sources of the fused kernels (phases 0 and 1, "" for a phase without fields) that
+    step these batched solvers together; no GPU needed."""
+    lib = capi.load()
+    arr = (C.c_void_p * len(solvers))(*[s.h for s in solvers])
+    out = []
+    for ph in (0, 1):
+        n = capi.check(lib.cupssgb_multi_generated_source(arr, len(solvers), ph, None, 0))
+        buf = C.create_string_buffer(n + 1)
+        lib.cupssgb_multi_generated_source(arr, len(solvers), ph, buf, n + 1)
+        out.append(buf.value.decode())
+    return out
+
+
 class Ensemble:
     """Mirror of the C++ ``ensemble`` (include/cupss/ensemble.h): one system declared
     with the evolver's calls, many members (grid, dt, seed, parameter values) advanced

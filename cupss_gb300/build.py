@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = [
     "k_line_1024.cu", "k_line_512.cu", "k_line_256.cu", "k_line_128.cu", "k_line_small.cu", "k_line_r3.cu",
     "k_row.cu", "k_plane.cu", "k_misc.cu", "noalloc.cu",
-    "engine.cpp", "engine_batch.cpp", "capi.cpp", "jit.cpp",
+    "engine.cpp", "engine_batch.cpp", "engine_multi.cpp", "capi.cpp", "jit.cpp",
     "host_parser.cpp", "host_evolver.cpp", "host_field_term.cpp", "host_init.cpp", "host_utils.cpp",
     "host_ir.cpp", "host_ensemble.cpp", "host_server.cpp", "host_output.cpp", "tune_cache.cpp",
 ]
@@ -35,7 +35,7 @@ def nvcc_path():
 
 
 JIT_HEADERS = ["engine_types.h", "twiddle32.h", "fft.cuh", "philox.cuh", "point_math.cuh",
-               "line_geom.cuh", "turn.cuh"]
+               "line_geom.cuh", "turn.cuh", "kernels.cuh"]
 
 
 def write_jit_headers():

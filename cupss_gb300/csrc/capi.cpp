@@ -11,6 +11,7 @@
 #include "../../include/cupss/server.h"
 #include "../../include/cupss_gb300.h"
 #include "engine.h"
+#include "engine_multi.h"
 #include "host_common.h"
 #include "jit.h"
 #include "tune_cache.h"
@@ -29,6 +30,10 @@ struct cupssgb_ensemble {
 
 struct cupssgb_server {
   server* s;
+};
+
+struct cupssgb_multi {
+  cupssgb::MultiStep* m;
 };
 
 namespace {
@@ -415,6 +420,68 @@ int cupssgb_tune_cache_store(const char* key, const char* value) {
   NEED(value);
   if (!cupssgb::tune_cache_store(key, value)) return fail(CUPSSGB_ERR_INVALID, "tune cache not written");
   return 0;
+}
+
+namespace {
+std::vector<cupssgb::Solver*> solvers_of(cupssgb_solver* const* solvers, int n) {
+  if (!solvers || n < 1) throw cupssgb::Error(CUPSSGB_ERR_INVALID, "no solvers");
+  std::vector<cupssgb::Solver*> v;
+  for (int i = 0; i < n; ++i) {
+    if (!solvers[i]) throw cupssgb::Error(CUPSSGB_ERR_INVALID, "null solver");
+    v.push_back(solvers[i]->s);
+  }
+  return v;
+}
+}  // namespace
+
+int cupssgb_multi_check(cupssgb_solver* const* solvers, int n, char* buf, int buflen) {
+  return guard([&] {
+    const std::string why = cupssgb::MultiStep::unsupported(solvers_of(solvers, n));
+    copy_out(why, buf, buflen);
+    return why.empty() ? 0 : fail(CUPSSGB_ERR_UNSUPPORTED, why);
+  });
+}
+
+int cupssgb_multi_create(cupssgb_solver* const* solvers, int n, cupssgb_multi** out) {
+  NEED(out);
+  return guard([&] {
+    *out = new cupssgb_multi{new cupssgb::MultiStep(solvers_of(solvers, n))};
+    return 0;
+  });
+}
+
+int cupssgb_multi_destroy(cupssgb_multi* m) {
+  if (!m) return 0;
+  return guard([&] {
+    delete m->m;
+    delete m;
+    return 0;
+  });
+}
+
+int cupssgb_multi_advance(cupssgb_multi* m, int nsteps) {
+  NEED(m);
+  return guard([&] {
+    m->m->advance(nsteps);
+    return 0;
+  });
+}
+
+long long cupssgb_multi_launch_count(const cupssgb_multi* m) { return m ? m->m->launches() : -1; }
+
+int cupssgb_multi_describe(const cupssgb_multi* m, char* buf, int buflen) {
+  NEED(m);
+  return copy_out(m->m->describe(), buf, buflen);
+}
+
+int cupssgb_multi_generated_source(cupssgb_solver* const* solvers, int n, int phase, char* buf, int buflen) {
+  std::string src;
+  const int rc = guard([&] {
+    src = cupssgb::MultiStep::generated_source(solvers_of(solvers, n), phase);
+    return 0;
+  });
+  if (rc != 0) return rc;
+  return copy_out(src, buf, buflen);
 }
 
 int cupssgb_set_device(int device) {

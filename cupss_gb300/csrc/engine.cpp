@@ -296,6 +296,12 @@ static int sm_count() {
   return v;
 }
 
+int Solver::phase_turn_w(const Phase& P, int nslots) const {
+  if (P.tuned_w > 0) return P.tuned_w;
+  const int W = pick_w(turn_len(), dim_ == 3 ? 2 : 1, nslots, turn_rows(), phase_split(P));
+  return (turn_w_ > 0 && turn_w_ < W) ? turn_w_ : W;
+}
+
 bool Solver::phase_split(const Phase& P) const {
   if (!use_jit_ || turn_len() < 512) return false;
   if (P.tuned_split >= 0 && split_override() < 0) return P.tuned_split == 1;
@@ -862,31 +868,7 @@ void Solver::run_phase(Phase& P) {
   // ---- row pass: real-space products of the dealiased copies ----
   if (!P.products.empty() && !plane_) {
     XParams x;
-    std::memset(&x, 0, sizeof(x));
-    x.Lx = Lx_;
-    x.rows = sy_ * sz_;
-    x.in_mode = kXInSpectral;
-    x.out_mode = kXOutSpectral;
-    x.out_scale = 1.f;
-    x.n_in = (int)P.xin.size();
-    for (int i = 0; i < x.n_in; ++i) {
-      const int g = P.xin[i];
-      x.in[i] = chan_[g];
-      // columns beyond the dealias limit of the channel are zero: not read
-      x.in_xcols[i] = chan_wide_[g] ? 0 : std::min(Lx_, sx_ / (alias_order_[g] + 1) + 1);
-    }
-    x.n_prod = (int)P.products.size();
-    for (int q = 0; q < x.n_prod; ++q) {
-      x.out[q] = P.prodbuf[q];
-      x.prod_n[q] = (int)P.products[q].size();
-      for (int t = 0; t < x.prod_n[q]; ++t) {
-        const int g = P.products[q][t];
-        x.prod_f[q][t] = (int)(std::find(P.xin.begin(), P.xin.end(), g) - P.xin.begin());
-      }
-    }
-    x.tw = tw_;
-    x.members = members_d_;
-    if (batch_) x.mstride = half_;
+    row_params(P, x);
     mark_begin();
     check(launch_row_pass(x, stream_, batch_ ? mspan_ : 1, pdl_), "row pass");
     mark_end("row_pass");
@@ -907,9 +889,7 @@ void Solver::run_phase(Phase& P) {
   int nslots = 0;
   bool any_chan = false;
   fill_turn(P, p, nslots, any_chan);
-  p.W = pick_w(L, nl, nslots, turn_rows(), phase_split(P));
-  if (turn_w_ > 0 && turn_w_ < p.W) p.W = turn_w_;
-  if (P.tuned_w > 0) p.W = P.tuned_w;
+  p.W = phase_turn_w(P, nslots);
   p.members = members_d_;
   p.step_off = step_off_;
   if (batch_) {
@@ -947,6 +927,34 @@ void Solver::run_phase(Phase& P) {
         mark_end("line_inv_y");
       }
   }
+}
+
+void Solver::row_params(const Phase& P, XParams& x) const {
+  std::memset(&x, 0, sizeof(x));
+  x.Lx = Lx_;
+  x.rows = sy_ * sz_;
+  x.in_mode = kXInSpectral;
+  x.out_mode = kXOutSpectral;
+  x.out_scale = 1.f;
+  x.n_in = (int)P.xin.size();
+  for (int i = 0; i < x.n_in; ++i) {
+    const int g = P.xin[i];
+    x.in[i] = g < (int)chan_.size() ? chan_[g] : nullptr;   // no buffers before prepare (source generation)
+    // columns beyond the dealias limit of the channel are zero: not read
+    x.in_xcols[i] = chan_wide_[g] ? 0 : std::min(Lx_, sx_ / (alias_order_[g] + 1) + 1);
+  }
+  x.n_prod = (int)P.products.size();
+  for (int q = 0; q < x.n_prod; ++q) {
+    x.out[q] = q < (int)P.prodbuf.size() ? P.prodbuf[q] : nullptr;
+    x.prod_n[q] = (int)P.products[q].size();
+    for (int t = 0; t < x.prod_n[q]; ++t) {
+      const int g = P.products[q][t];
+      x.prod_f[q][t] = (int)(std::find(P.xin.begin(), P.xin.end(), g) - P.xin.begin());
+    }
+  }
+  x.tw = tw_;
+  x.members = members_d_;
+  if (batch_) x.mstride = half_;
 }
 
 void Solver::mark_begin() {

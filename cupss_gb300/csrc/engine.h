@@ -141,6 +141,7 @@ class Solver {
   int alias_order(int f) const { return alias_order_.at(f); }
 
  private:
+  friend class MultiStep;   // engine_multi.cpp: fused launches over several batched solvers
   struct Phase {
     int id = 0;                              // 0: non-dynamic, 1: dynamic
     std::vector<int> fields;                 // fields updated in this phase
@@ -161,6 +162,8 @@ class Solver {
   void* dalloc(size_t bytes);
   void build_plan();
   void run_phase(Phase& ph);
+  // the row pass of a phase with products (its products from the dealiased channels)
+  void row_params(const Phase& P, XParams& x) const;
   void fill_turn(const Phase& P, LineParams& p, int& nslots, bool& any_chan,
                  const std::vector<HostField>* fields = nullptr) const;
   const std::string& turn_source(Phase& P, const LineParams& p, int L, int nl);
@@ -172,6 +175,8 @@ class Solver {
   // the phase's turnaround runs the generated kernel with lines in the split FFT form
   bool phase_split(const Phase& P) const;
   int phase_warps(const Phase& P) const { return P.tuned_warps > 0 ? P.tuned_warps : turn_warps_; }
+  // turnaround tile width of a phase: the tuned one, else the rule (and CUPSSGB_TURN_W)
+  int phase_turn_w(const Phase& P, int nslots) const;
   int turn_len() const { return dim_ == 3 ? sz_ : sy_; }
   // autotuner: cache key of a phase, its value string, and applying a cached value
   std::string tune_key(const Phase& P);

@@ -1,0 +1,70 @@
+// Fused stepping of several batched solvers of one system structure on different grids.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+
+namespace cupssgb {
+
+// Batched solvers ("grid classes") of one system structure on different 1D/2D grids,
+// stepped together: every kernel of a step is one launch over all of them.  The fused
+// turnaround and row pass are generated per set of classes (jit_generate_multi): each
+// class's body is specialised to its grid, owns a contiguous range of blockIdx.x and sees
+// its own members at blockIdx.z, so per-member data and noise are exactly those of the
+// class's own launches -- a member's trajectory is the one it has in its own solver.
+// Steps are replayed from CUDA graphs of 16, 4 and 1 steps.  The classes keep their
+// buffers, member tables and set/get calls; stepping runs on this object's stream, which
+// waits for the classes' streams before each advance (and they for it after).
+class MultiStep {
+ public:
+  // "" when the solvers can be stepped fused, else the reason they cannot.  With
+  // need_prepared false, unprepared solvers have their plans built (no GPU needed).
+  static std::string unsupported(const std::vector<Solver*>& s, bool need_prepared = true);
+  // Source of the fused kernels of phase ph (0 non-dynamic, 1 dynamic; "" when the phase
+  // has no fields): needs no GPU.
+  static std::string generated_source(const std::vector<Solver*>& s, int ph);
+  explicit MultiStep(const std::vector<Solver*>& s);
+  ~MultiStep();
+  MultiStep(const MultiStep&) = delete;
+  MultiStep& operator=(const MultiStep&) = delete;
+  void advance(int nsteps);
+  long long launches() const { return launches_; }
+  std::string describe() const;   // JSON: per class grid, tile width, CTAs
+
+ private:
+  struct PhaseK {
+    bool active = false, has_row = false;
+    cudaKernel_t turn = nullptr, row = nullptr;
+    int turn_threads = 0;   // threads of a fused turnaround CTA: W_c * M_c for every class c
+    size_t turn_smem = 0, row_smem = 0;
+    dim3 turn_grid, row_grid;
+    std::vector<int> turn_w, turn_tiles, row_blocks;
+  };
+  // Launch shapes of phase ph and (src != nullptr) the source of its fused kernels;
+  // "" when every class fits them, else the reason.
+  static std::string plan_phase(const std::vector<Solver*>& s, int ph, PhaseK& K, std::string* src);
+  void check(cudaError_t e, const char* what);
+  void build();
+  void launch_phase(int ph, uint32_t off);
+  void step_once(uint32_t off, bool tick);
+  void capture(int c, int parity);
+
+  std::vector<Solver*> s_;
+  PhaseK ph_[2];
+  cudaStream_t stream_ = nullptr;
+  cudaEvent_t ev_ = nullptr;
+  std::vector<cudaEvent_t> class_ev_;
+  cudaGraphExec_t graph_[3][2] = {};
+  std::vector<int> graph_span_;   // the classes' member spans the graphs were captured with
+  long long graph_launches_[3] = {};
+  long long launches_ = 0;
+  // parameter blocks of the fused launches (27 KB and 4 KB), built per launch
+  std::unique_ptr<MultiTurnParams> mt_;
+  std::unique_ptr<MultiRowParams> mr_;
+};
+
+}  // namespace cupssgb

@@ -145,6 +145,25 @@ struct PlaneParams {
   const MemberK* members;
 };
 
+// Fused launches over several batched solvers of one system structure on different grids
+// ("grid classes"): class c owns a contiguous range of blockIdx.x and its members are
+// blockIdx.z < span[c].  Passed by value (8 LineParams stay below the 32 KB parameter limit).
+constexpr int kMaxClasses = 8;
+struct MultiTurnParams {
+  LineParams p[kMaxClasses];
+  int span[kMaxClasses];
+};
+struct MultiRowParams {
+  XParams x[kMaxClasses];
+  int span[kMaxClasses];
+};
+struct MultiTickParams {
+  MemberK* members[kMaxClasses];
+  int n[kMaxClasses];
+  int nc;
+  uint32_t inc;
+};
+
 struct ExpandParams {
   int sx, sy, sz, Lx;
   const float2* spec;   // packed half spectrum, fully transformed

@@ -2,6 +2,7 @@
 // include/cupss/ensemble.h).  Errors throw std::runtime_error / ParseError.
 #include "../../include/cupss/ensemble.h"
 
+#include <cstdlib>
 #include <map>
 #include <sstream>
 #include <stdexcept>
@@ -34,6 +35,10 @@ struct ensemble::Impl {
   std::vector<Member> members;
   std::vector<Group> groups;
   bool prepared = false;
+  // every group stepped by one fused launch per kernel (1D/2D grids of one structure);
+  // null when the groups do not qualify or CUPSSGB_FUSE=0
+  cupssgb_multi* multi = nullptr;
+  std::string multi_why;
 
   int field_index(const std::string& name) const {
     for (size_t i = 0; i < fields.size(); ++i)
@@ -52,6 +57,7 @@ struct ensemble::Impl {
 ensemble::ensemble() : impl_(new Impl) {}
 
 ensemble::~ensemble() {
+  if (impl_->multi) cupssgb_multi_destroy(impl_->multi);
   for (auto& g : impl_->groups)
     if (g.solver) cupssgb_solver_destroy(g.solver);
   delete impl_;
@@ -148,6 +154,21 @@ void ensemble::prepare() {
       cupssgb_host::set_member(g.solver, (int)k, irs[g.members[k]], I.members[g.members[k]].seed);
     ok(cupssgb_solver_prepare(g.solver));
   }
+  // one launch per kernel and step across every grid size, where the groups allow it
+  const char* fuse = std::getenv("CUPSSGB_FUSE");
+  if (I.groups.size() < 2) {
+    I.multi_why = "one grid class: stepped by its own tuned graphs";
+  } else if (!(fuse && std::string(fuse) == "0")) {
+    std::vector<cupssgb_solver*> sv;
+    for (Impl::Group& g : I.groups) sv.push_back(g.solver);
+    char why[256] = {0};
+    if (cupssgb_multi_check(sv.data(), (int)sv.size(), why, (int)sizeof(why)) == 0)
+      ok(cupssgb_multi_create(sv.data(), (int)sv.size(), &I.multi));
+    else
+      I.multi_why = why;
+  } else {
+    I.multi_why = "CUPSSGB_FUSE=0";
+  }
   I.prepared = true;
 }
 
@@ -162,8 +183,13 @@ int ensemble::setReal(int member, const std::string& field, const float* host_re
 int ensemble::advance(int nsteps) {
   Impl& I = *impl_;
   if (!I.prepared) throw std::runtime_error("advance before prepare");
-  // each group queues its steps on its own stream; they run concurrently
-  for (Impl::Group& g : I.groups) ok(cupssgb_solver_advance(g.solver, nsteps));
+  if (I.multi) {
+    // one launch per kernel and step over every group; the groups' streams wait for it
+    ok(cupssgb_multi_advance(I.multi, nsteps));
+  } else {
+    // each group queues its steps on its own stream; they run concurrently
+    for (Impl::Group& g : I.groups) ok(cupssgb_solver_advance(g.solver, nsteps));
+  }
   for (Impl::Group& g : I.groups) ok(cupssgb_solver_synchronize(g.solver));
   return 0;
 }
@@ -188,8 +214,11 @@ long long ensemble::deviceBytes() const {
 long long ensemble::launches() const {
   long long n = 0;
   for (const auto& g : impl_->groups) n += cupssgb_solver_launch_count(g.solver);
+  if (impl_->multi) n += cupssgb_multi_launch_count(impl_->multi);
   return n;
 }
+
+bool ensemble::fused() const { return impl_->multi != nullptr; }
 
 std::string ensemble::describe() const {
   std::ostringstream os;
@@ -210,5 +239,11 @@ std::string ensemble::describe() const {
        << ", \"members\": " << g.members.size() << ", \"tune\": " << (tune.empty() ? "{}" : tune) << "}";
   }
   os << "]";
-  return os.str();
+  if (impl_->multi) {
+    const int n = cupssgb_multi_describe(impl_->multi, nullptr, 0);
+    std::vector<char> buf(n + 1);
+    cupssgb_multi_describe(impl_->multi, buf.data(), n + 1);
+    return "{\"groups\": " + os.str() + ", \"fused\": " + buf.data() + "}";
+  }
+  return "{\"groups\": " + os.str() + ", \"fused\": null, \"why_not_fused\": \"" + impl_->multi_why + "\"}";
 }

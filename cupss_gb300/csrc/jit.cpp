@@ -5,9 +5,9 @@
 // is fixed once the equations are parsed.  The engine emits it as straight-line CUDA
 // (numerical prefactor values stay in the kernel parameter block, so updateParameter
 // needs no recompilation), compiles it for the running GPU with NVRTC and launches the
-// cubin through the runtime's library API.  Compiled kernels are cached per process by
-// device and source text: each device gets a build for its own architecture, with the
-// shared-memory limit raised on that device.
+// cubin through the runtime's library API.  Compiled libraries are cached per process by
+// device and source text, kernels by device, source and entry point: each device gets a
+// build for its own architecture, with the shared-memory limit raised on that device.
 #include "jit.h"
 
 #include <nvrtc.h>
@@ -34,7 +34,8 @@ namespace {
 const char* const kJitFastOpts[] = {"--prec-div=false", "--prec-sqrt=false"};
 
 std::mutex g_mu;
-std::map<std::pair<int, std::string>, cudaKernel_t> g_cache;   // (device, source) -> kernel
+std::map<std::pair<int, std::string>, cudaLibrary_t> g_libs;   // (device, source) -> loaded library
+std::map<std::pair<int, std::string>, cudaKernel_t> g_cache;   // (device, source + entry) -> kernel
 
 std::string pow_expr(const char* base, int n) {
   if (n <= 0) return "";
@@ -62,7 +63,10 @@ std::string keep_expr(int s, const PresK& p, bool* never) {
 
 }  // namespace
 
-std::string jit_generate_turn(const LineParams& p, int L, int NL, int warps, bool batched, bool split_form) {
+namespace {
+
+// struct GenProg: the update program of the phase described by p (see jit_generate_turn).
+std::string gen_prog(const LineParams& p, bool batched) {
   // numerical values: the parameter block (one system) or the batch member's row
   auto pre = [&](int k) {
     return batched ? "__ldg(mv + " + std::to_string(k) + ")" : "P.pres[" + std::to_string(k) + "].pre";
@@ -71,19 +75,8 @@ std::string jit_generate_turn(const LineParams& p, int L, int NL, int warps, boo
     return batched ? "__ldg(mv + kMaxPres + " + std::to_string(fi) + ")"
                    : "P.f[" + std::to_string(fi) + "].noise_base";
   };
-  // block = (W, M, NL) threads
-  const bool split = split_form && L >= 512;
-  const int M = line_threads(L, 1, 1, split);   // LineCfg<L, split>::M
-  const int threads = p.W > 0 ? p.W * M * NL : 256;
-  const int min_blocks = std::max(1, warps * 32 / threads);
-  // overlap of the first field's noise with the first product's loads: for spectra that
-  // do not stay in the L2 (64 MB and more per array); CUPSSGB_EARLY_NOISE=0/1 overrides
-  bool early_noise = (double)p.Lx * p.sy * p.sz * 8.0 >= 64.0 * 1024 * 1024;
-  if (const char* e = std::getenv("CUPSSGB_EARLY_NOISE")) early_noise = std::string(e) == "1";
   std::ostringstream o;
-  o << "#include \"turn.cuh\"\n"
-    << "namespace cupssgb {\n"
-    << "struct GenProg {\n"
+  o << "struct GenProg {\n"
     << "  static constexpr bool kUnroll = true;\n"
     << "  template <class F>\n"
     << "  __device__ __forceinline__ static float2 eval(const LineParams& P, int fi, const VPoint& vp, "
@@ -160,19 +153,92 @@ std::string jit_generate_turn(const LineParams& p, int L, int NL, int warps, boo
     }
     o << "        return nv;\n      }\n";
   }
-  o << "    }\n    return make_float2(0.f, 0.f);\n  }\n};\n"
-    // the phase structure and grid this kernel is specialised for
-    << "struct GenSpec {\n"
+  o << "    }\n    return make_float2(0.f, 0.f);\n  }\n};\n";
+  return o.str();
+}
+
+// struct <name>: the phase structure and grid a turnaround is specialised for.
+std::string gen_spec(const LineParams& p, const std::string& name, bool early_noise, bool split) {
+  std::ostringstream o;
+  o << "struct " << name << " {\n"
     << "  static constexpr int kNF = " << p.nf << ";\n"
     << "  static constexpr int kNProd = " << p.n_prod << ";\n"
     << "  static constexpr int kSX = " << p.sx << ", kSY = " << p.sy << ", kSZ = " << p.sz << ";\n"
     << "  static constexpr int kW = " << p.W << ";\n"
     << "  static constexpr bool kEarlyNoise = " << (early_noise ? "true" : "false") << ";\n"
     << "  static constexpr bool kSplit = " << (split ? "true" : "false") << ";\n"
-    << "};\n}  // namespace cupssgb\n"
+    << "};\n";
+  return o.str();
+}
+
+// overlap of the first field's noise with the first product's loads: for spectra that
+// do not stay in the L2 (64 MB and more per array); CUPSSGB_EARLY_NOISE=0/1 overrides
+bool early_noise_for(const LineParams& p) {
+  bool early = (double)p.Lx * p.sy * p.sz * 8.0 >= 64.0 * 1024 * 1024;
+  if (const char* e = std::getenv("CUPSSGB_EARLY_NOISE")) early = std::string(e) == "1";
+  return early;
+}
+
+}  // namespace
+
+std::string jit_generate_turn(const LineParams& p, int L, int NL, int warps, bool batched, bool split_form) {
+  // block = (W, M, NL) threads
+  const bool split = split_form && L >= 512;
+  const int M = line_threads(L, 1, 1, split);   // LineCfg<L, split>::M
+  const int threads = p.W > 0 ? p.W * M * NL : 256;
+  const int min_blocks = std::max(1, warps * 32 / threads);
+  std::ostringstream o;
+  o << "#include \"turn.cuh\"\n"
+    << "namespace cupssgb {\n"
+    << gen_prog(p, batched) << gen_spec(p, "GenSpec", early_noise_for(p), split)
+    << "}  // namespace cupssgb\n"
     << "extern \"C\" __global__ void __launch_bounds__(" << threads << ", " << min_blocks
     << ") cupssgb_turn(const cupssgb::LineParams P) {\n"
     << "  cupssgb::turn_body<" << L << ", " << NL << ", cupssgb::GenProg, cupssgb::GenSpec>(P);\n}\n";
+  return o.str();
+}
+
+std::string jit_program_text(const LineParams& p, bool batched) { return gen_prog(p, batched); }
+
+std::string jit_generate_multi(const std::vector<MultiClassSpec>& cls, bool has_row, bool batched, int turn_threads,
+                               int turn_min_blocks, int row_min_blocks) {
+  std::ostringstream o;
+  o << "#include \"turn.cuh\"\n#include \"kernels.cuh\"\nnamespace cupssgb {\n" << gen_prog(cls[0].turn, batched);
+  for (size_t c = 0; c < cls.size(); ++c)
+    o << gen_spec(cls[c].turn, "GenSpec" + std::to_string(c), early_noise_for(cls[c].turn), cls[c].split);
+  o << "}  // namespace cupssgb\n";
+  // turnaround: flat blocks of turn_threads = W_c * M_c threads
+  o << "extern \"C\" __global__ void __launch_bounds__(" << turn_threads << ", " << turn_min_blocks
+    << ") cupssgb_turn_multi(const cupssgb::MultiTurnParams MP) {\n"
+    << "  const int bx = blockIdx.x;\n  const int tid = threadIdx.x;\n";
+  int b0 = 0;
+  for (size_t c = 0; c < cls.size(); ++c) {
+    const int b1 = b0 + cls[c].turn_tiles;
+    const int W = cls[c].turn.W;
+    o << "  " << (c ? "else " : "") << "if (bx < " << b1 << ") {\n"
+      << "    if ((int)blockIdx.z >= MP.span[" << c << "]) return;\n"
+      << "    cupssgb::turn_body_at<" << cls[c].L << ", 1, cupssgb::GenProg, cupssgb::GenSpec" << c << ">(MP.p[" << c
+      << "], bx - " << b0 << ", 0, tid % " << W << ", tid / " << W << ", 0);\n  }\n";
+    b0 = b1;
+  }
+  o << "}\n";
+  if (has_row) {
+    o << "extern \"C\" __global__ void __launch_bounds__(128, " << row_min_blocks
+      << ") cupssgb_row_multi(const cupssgb::MultiRowParams MP) {\n"
+      << "  const int bx = blockIdx.x;\n  const int tid = threadIdx.x;\n";
+    b0 = 0;
+    for (size_t c = 0; c < cls.size(); ++c) {
+      const int b1 = b0 + cls[c].row_blocks;
+      const int M = cls[c].row_m;
+      o << "  " << (c ? "else " : "") << "if (bx < " << b1 << ") {\n"
+        << "    if ((int)blockIdx.z >= MP.span[" << c << "]) return;\n"
+        << "    cupssgb::" << (cls[c].row_one ? "row_one_body" : "row_pass_body") << "<" << cls[c].LX << ", "
+        << (cls[c].row_split ? "true" : "false") << ">(MP.x[" << c << "], bx - " << b0 << ", tid % " << M
+        << ", tid / " << M << ");\n  }\n";
+      b0 = b1;
+    }
+    o << "}\n";
+  }
   return o.str();
 }
 
@@ -181,41 +247,48 @@ cudaKernel_t jit_kernel(const std::string& source, const char* entry) {
   int dev = 0, major = 0, minor = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) throw Error(kErrCuda, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-  auto it = g_cache.find({dev, source});
+  const std::pair<int, std::string> kkey{dev, source + '\n' + entry};
+  auto it = g_cache.find(kkey);
   if (it != g_cache.end()) return it->second;
-  if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess ||
-      cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev) != cudaSuccess)
-    throw Error(kErrCuda, "compute capability query failed");
-  // sm_103a on GB300; other Blackwell parts get their own arch-specific target
-  const std::string arch = "--gpu-architecture=sm_" + std::to_string(major * 10 + minor) + "a";
-  nvrtcProgram prog;
-  if (nvrtcCreateProgram(&prog, source.c_str(), "cupssgb_turn.cu", kJitNumHeaders, kJitHeaderSources,
-                         kJitHeaderNames) != NVRTC_SUCCESS)
-    throw Error(kErrCuda, "nvrtcCreateProgram failed");
-  const char* opts[] = {arch.c_str(), "--std=c++17", "-lineinfo", kJitFastOpts[0], kJitFastOpts[1]};
-  const nvrtcResult rc = nvrtcCompileProgram(prog, 5, opts);
-  if (rc != NVRTC_SUCCESS) {
+  cudaLibrary_t lib = nullptr;
+  auto lit = g_libs.find({dev, source});
+  if (lit != g_libs.end()) {
+    lib = lit->second;
+  } else {
+    if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev) != cudaSuccess)
+      throw Error(kErrCuda, "compute capability query failed");
+    // sm_103a on GB300; other Blackwell parts get their own arch-specific target
+    const std::string arch = "--gpu-architecture=sm_" + std::to_string(major * 10 + minor) + "a";
+    nvrtcProgram prog;
+    if (nvrtcCreateProgram(&prog, source.c_str(), "cupssgb_turn.cu", kJitNumHeaders, kJitHeaderSources,
+                           kJitHeaderNames) != NVRTC_SUCCESS)
+      throw Error(kErrCuda, "nvrtcCreateProgram failed");
+    const char* opts[] = {arch.c_str(), "--std=c++17", "-lineinfo", kJitFastOpts[0], kJitFastOpts[1]};
+    const nvrtcResult rc = nvrtcCompileProgram(prog, 5, opts);
+    if (rc != NVRTC_SUCCESS) {
+      size_t n = 0;
+      nvrtcGetProgramLogSize(prog, &n);
+      std::string log(n, '\0');
+      nvrtcGetProgramLog(prog, &log[0]);
+      nvrtcDestroyProgram(&prog);
+      throw Error(kErrCuda, "NVRTC compilation of the update program failed:\n" + log);
+    }
     size_t n = 0;
-    nvrtcGetProgramLogSize(prog, &n);
-    std::string log(n, '\0');
-    nvrtcGetProgramLog(prog, &log[0]);
+    nvrtcGetCUBINSize(prog, &n);
+    std::vector<char> cubin(n);
+    nvrtcGetCUBIN(prog, cubin.data());
     nvrtcDestroyProgram(&prog);
-    throw Error(kErrCuda, "NVRTC compilation of the update program failed:\n" + log);
+    e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+    if (e != cudaSuccess) throw Error(kErrCuda, std::string("cudaLibraryLoadData: ") + cudaGetErrorString(e));
+    g_libs[{dev, source}] = lib;
   }
-  size_t n = 0;
-  nvrtcGetCUBINSize(prog, &n);
-  std::vector<char> cubin(n);
-  nvrtcGetCUBIN(prog, cubin.data());
-  nvrtcDestroyProgram(&prog);
-  cudaLibrary_t lib;
-  e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
-  if (e != cudaSuccess) throw Error(kErrCuda, std::string("cudaLibraryLoadData: ") + cudaGetErrorString(e));
   cudaKernel_t k;
   e = cudaLibraryGetKernel(&k, lib, entry);
   if (e != cudaSuccess) throw Error(kErrCuda, std::string("cudaLibraryGetKernel: ") + cudaGetErrorString(e));
   e = cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
   if (e != cudaSuccess) throw Error(kErrCuda, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
-  g_cache[{dev, source}] = k;
+  g_cache[kkey] = k;
   return k;
 }
 

@@ -137,6 +137,21 @@ cudaError_t launch_tick(MemberK* members, int n, uint32_t inc, cudaStream_t st, 
   return cudaLaunchKernelEx(&lc.cfg, tick_members, members, n, inc);
 }
 
+// blockIdx.y = grid class
+__global__ void tick_members_multi(const MultiTickParams p) {
+  grid_dep_sync();
+  const int c = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < p.nc && i < p.n[c] && p.members[c][i].active) p.members[c][i].step += p.inc;
+}
+
+cudaError_t launch_tick_multi(const MultiTickParams& p, cudaStream_t st, bool pdl) {
+  int nmax = 1;
+  for (int c = 0; c < p.nc; ++c) nmax = p.n[c] > nmax ? p.n[c] : nmax;
+  LaunchCfg lc(dim3((nmax + 255) / 256, p.nc), dim3(256), 0, st, pdl);
+  return cudaLaunchKernelEx(&lc.cfg, tick_members_multi, p);
+}
+
 cudaError_t launch_compress(const CompressParams& p, cudaStream_t st) {
   const size_t H = (size_t)p.Lx * p.sy * p.sz;
   int blocks = (int)((H + 255) / 256);

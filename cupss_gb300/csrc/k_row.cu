@@ -54,6 +54,44 @@ static cudaError_t launch_row_t(const XParams& p, cudaStream_t st, int nz, bool 
   return launch_row_form<LX, false>(p, st, nz, pdl);
 }
 
+template <int LX, bool SP>
+static RowShape row_shape_form(const XParams& p) {
+  using C = RowCfg<LX, SP>;
+  RowShape r;
+  r.one = row_is_one(p);
+  r.split = SP;
+  r.m = C::M;
+  r.rw = C::RW;
+  r.smem = (r.one ? 2 : (size_t)(1 + p.n_in)) * C::RW * C::PL * sizeof(float2);
+  r.blocks = (p.rows + C::RW - 1) / C::RW;
+  return r;
+}
+
+template <int LX>
+static RowShape row_shape_t(const XParams& p, int nz) {
+  if constexpr (LX >= 512) {
+    if (row_split(LX, (long long)p.rows * nz)) return row_shape_form<LX, true>(p);
+  }
+  return row_shape_form<LX, false>(p);
+}
+
+RowShape row_pass_shape(const XParams& p, int nz) {
+  switch (p.Lx) {
+    case 16: return row_shape_t<16>(p, nz);
+    case 32: return row_shape_t<32>(p, nz);
+    case 64: return row_shape_t<64>(p, nz);
+    case 128: return row_shape_t<128>(p, nz);
+    case 256: return row_shape_t<256>(p, nz);
+    case 512: return row_shape_t<512>(p, nz);
+    case 1024: return row_shape_t<1024>(p, nz);
+    case 24: return row_shape_t<24>(p, nz);
+    case 48: return row_shape_t<48>(p, nz);
+    case 96: return row_shape_t<96>(p, nz);
+    case 192: return row_shape_t<192>(p, nz);
+    default: return RowShape{false, false, 0, 0, 0, 0};
+  }
+}
+
 cudaError_t launch_row_pass(const XParams& p, cudaStream_t st, int nz, bool pdl) {
   switch (p.Lx) {
     case 1: return launch_row_t<1>(p, st, nz, pdl);

@@ -14,8 +14,10 @@
 //                   mask (dealias_k, :229-256) and 1/N normalisation (normalize_k,
 //                   :115-128), and the inverse FFT of the dealiased copies.
 #pragma once
+#if !defined(__CUDACC_RTC__)
 #include <cuda_runtime.h>
 #include <cstdint>
+#endif
 #include "engine_types.h"
 #include "fft.cuh"
 #include "philox.cuh"
@@ -89,6 +91,37 @@ __device__ __forceinline__ float2 row_twiddle(float2 wm) {
   return tw_const<2 * R, step2_off<LX, SP>(I) / M, false>(wm);
 }
 
+// Register i of the two loops below, i a compile-time index (a functor rather than a
+// lambda: the generated kernels that include this header are compiled by NVRTC, which
+// treats lambdas without an execution-space annotation as host code).
+template <int LX, bool SP>
+struct RowC2rAt {
+  float2 (&v)[LineCfg<LX, SP>::R];
+  const float2* T;
+  int m;
+  float2 wm;
+  template <int i>
+  __device__ __forceinline__ void operator()(ic<i>) const {
+    const int k = pos_step2<LX, SP>(m, i);
+    v[i] = c2r_pre_w(v[i], T[pad_pos<LX, SP>(neg_mod(k, LX))], k, row_twiddle<LX, SP, i>(wm));
+  }
+};
+template <int LX, bool SP>
+struct RowR2cAt {
+  const float2 (&v)[LineCfg<LX, SP>::R];
+  const float2* T;
+  int m;
+  float2 wm;
+  float2* out;
+  bool live;
+  template <int i>
+  __device__ __forceinline__ void operator()(ic<i>) const {
+    const int k = pos_step2<LX, SP>(m, i);
+    const float2 x = r2c_post_w(v[i], T[pad_pos<LX, SP>(neg_mod(k, LX))], k, row_twiddle<LX, SP, i>(wm));
+    if (live) out[k] = x;
+  }
+};
+
 // C2R pre-processing of a packed row held in step-2 layout (v) and also stored in T
 // (padded positions): v[i] <- Z at k = pos_step2(m, i), the mirror X[Lx - k] from T.
 template <int LX, bool SP>
@@ -96,11 +129,7 @@ __device__ __forceinline__ void row_c2r(float2 (&v)[LineCfg<LX, SP>::R], const f
   constexpr int R = LineCfg<LX, SP>::R, sx = 2 * LX;
   if constexpr (RowTwSplit<LX, SP>::value) {
     const float2 wm = tw_load(tw, sx, m);
-    static_for(make_iseq<R>{}, [&](auto I) {
-      constexpr int i = decltype(I)::value;
-      const int k = pos_step2<LX, SP>(m, i);
-      v[i] = c2r_pre_w(v[i], T[pad_pos<LX, SP>(neg_mod(k, LX))], k, row_twiddle<LX, SP, i>(wm));
-    });
+    static_for(make_iseq<R>{}, RowC2rAt<LX, SP>{v, T, m, wm});
   } else {
 #pragma unroll
     for (int i = 0; i < R; ++i) {
@@ -118,12 +147,7 @@ __device__ __forceinline__ void row_r2c_store(const float2 (&v)[LineCfg<LX, SP>:
   constexpr int R = LineCfg<LX, SP>::R, sx = 2 * LX;
   if constexpr (RowTwSplit<LX, SP>::value) {
     const float2 wm = tw_load(tw, sx, m);
-    static_for(make_iseq<R>{}, [&](auto I) {
-      constexpr int i = decltype(I)::value;
-      const int k = pos_step2<LX, SP>(m, i);
-      const float2 x = r2c_post_w(v[i], T[pad_pos<LX, SP>(neg_mod(k, LX))], k, row_twiddle<LX, SP, i>(wm));
-      if (live) out[k] = x;
-    });
+    static_for(make_iseq<R>{}, RowR2cAt<LX, SP>{v, T, m, wm, out, live});
   } else {
 #pragma unroll
     for (int i = 0; i < R; ++i) {
@@ -147,16 +171,16 @@ struct RowCfg {
 };
 
 // smem: (1 + n_in) slots of RW*PL float2.  Slot 0 is the transpose buffer.
+// Row block bx, thread (m, rl): blockIdx.x and threadIdx in a plain launch; a fused launch
+// over several grids maps its flat indices to them.  The batch member is blockIdx.z.
 template <int LX, bool SP>
-__device__ __forceinline__ void row_pass_body(const XParams& p) {
+__device__ __forceinline__ void row_pass_body(const XParams& p, int bx, int m, int rl) {
   using C = RowCfg<LX, SP>;
   constexpr int M = C::M, R = C::R, PL = C::PL, RW = C::RW;
   extern __shared__ float2 smem[];
   grid_dep_sync();
   if (p.members && !p.members[blockIdx.z].active) return;   // CTA-uniform
-  const int m = threadIdx.x;
-  const int rl = threadIdx.y;
-  const int row = blockIdx.x * RW + rl;
+  const int row = bx * RW + rl;
   const bool live = row < p.rows;
   const int sx = 2 * LX;
   float2* T = smem + rl * PL;
@@ -270,11 +294,11 @@ __device__ __forceinline__ void row_pass_body(const XParams& p) {
 // without it the register allocation of the split form spills).
 template <int LX>
 __global__ void __launch_bounds__(RowCfg<LX, false>::M * RowCfg<LX, false>::RW) row_pass(const XParams p) {
-  row_pass_body<LX, false>(p);
+  row_pass_body<LX, false>(p, blockIdx.x, threadIdx.x, threadIdx.y);
 }
 template <int LX>
 __global__ void __launch_bounds__(RowCfg<LX, true>::M * RowCfg<LX, true>::RW, 2) row_pass_split(const XParams p) {
-  row_pass_body<LX, true>(p);
+  row_pass_body<LX, true>(p, blockIdx.x, threadIdx.x, threadIdx.y);
 }
 
 // Single spectral input, single spectral product (the Cahn-Hilliard form phi^n): the
@@ -289,16 +313,13 @@ struct RowOneCfg {
 };
 
 template <int LX, bool SP>
-__global__ void __launch_bounds__(RowCfg<LX, SP>::M * RowCfg<LX, SP>::RW, RowOneCfg<LX, SP>::kMinBlocks)
-row_pass_one(const XParams p) {
+__device__ __forceinline__ void row_one_body(const XParams& p, int bx, int m, int rl) {
   using C = RowCfg<LX, SP>;
   constexpr int M = C::M, R = C::R, PL = C::PL, RW = C::RW;
   extern __shared__ float2 smem[];
   grid_dep_sync();
   if (p.members && !p.members[blockIdx.z].active) return;   // CTA-uniform
-  const int m = threadIdx.x;
-  const int rl = threadIdx.y;
-  const int row = blockIdx.x * RW + rl;
+  const int row = bx * RW + rl;
   const bool live = row < p.rows;
   // two transpose buffers used in turn: a buffer is written again only after a barrier
   // that follows every read of its previous contents, so the write-after-read barriers
@@ -342,6 +363,12 @@ row_pass_one(const XParams p) {
   for (int i = 0; i < R; ++i) TB[pad_pos<LX, SP>(pos_step2<LX, SP>(m, i))] = v[i];
   __syncthreads();
   row_r2c_store<LX, SP>(v, TB, m, p.tw, reinterpret_cast<float2*>(p.out[0]) + rowoff, live);
+}
+
+template <int LX, bool SP>
+__global__ void __launch_bounds__(RowCfg<LX, SP>::M * RowCfg<LX, SP>::RW, RowOneCfg<LX, SP>::kMinBlocks)
+row_pass_one(const XParams p) {
+  row_one_body<LX, SP>(p, blockIdx.x, threadIdx.x, threadIdx.y);
 }
 
 // ------------------------------------------------------------------------------------

@@ -77,6 +77,18 @@ cudaError_t launch_compress(const CompressParams& p, cudaStream_t st);
 cudaError_t launch_mask(const MaskParams& p, cudaStream_t st);
 // Advances the step count of every active member by inc.
 cudaError_t launch_tick(MemberK* members, int n, uint32_t inc, cudaStream_t st, bool pdl = false);
+// The same for the member tables of several grid classes, in one launch.
+cudaError_t launch_tick_multi(const MultiTickParams& p, cudaStream_t st, bool pdl = false);
+// Row pass of a grid class as the fused launch runs it (the form launch_row_pass would pick for
+// nz members): single-input form, split form, threads per row (M), rows per CTA (RW), dynamic
+// shared memory and CTAs along x.
+struct RowShape {
+  bool one, split;
+  int m, rw;
+  size_t smem;
+  int blocks;
+};
+RowShape row_pass_shape(const XParams& p, int nz);
 
 // per-L launchers (one translation unit per group of sizes)
 #define CUPSSGB_DECL_LINE(L) \

@@ -38,14 +38,23 @@ struct LineGeom {
   int lofs, pstride;     // element offset of this thread's line (position 0) and stride, within a member
   size_t mbase;
   int slot_sz;
-  __device__ __forceinline__ explicit LineGeom(const LineParams& P) { init(P, P.sy, P.sx / 2, blockIdx.x, blockIdx.y); }
+  __device__ __forceinline__ explicit LineGeom(const LineParams& P) {
+    init(P, P.sy, P.sx / 2, blockIdx.x, blockIdx.y, threadIdx.x, threadIdx.y, threadIdx.z);
+  }
   // Grid sizes from the caller (compile-time constants in generated kernels).
-  __device__ __forceinline__ LineGeom(const LineParams& P, int sy, int Lx) { init(P, sy, Lx, blockIdx.x, blockIdx.y); }
-  __device__ __forceinline__ void init(const LineParams& P, int sy, int Lx, int tx, int ty) {
+  __device__ __forceinline__ LineGeom(const LineParams& P, int sy, int Lx) {
+    init(P, sy, Lx, blockIdx.x, blockIdx.y, threadIdx.x, threadIdx.y, threadIdx.z);
+  }
+  // Tile (tx, ty) and thread (w, m, l) given by the caller: a fused launch over several
+  // grids maps its flat block index and thread index to them.
+  __device__ __forceinline__ LineGeom(const LineParams& P, int sy, int Lx, int tx, int ty, int tw, int tm, int tl) {
+    init(P, sy, Lx, tx, ty, tw, tm, tl);
+  }
+  __device__ __forceinline__ void init(const LineParams& P, int sy, int Lx, int tx, int ty, int tw, int tm, int tl) {
     W = WT > 0 ? WT : P.W;
-    w = threadIdx.x;
-    m = threadIdx.y;
-    l = threadIdx.z;
+    w = tw;
+    m = tm;
+    l = tl;
     kx0 = tx * W;
     kxp = kx0 + w;
     lineky = 0;

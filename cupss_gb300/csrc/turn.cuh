@@ -202,8 +202,10 @@ __device__ __forceinline__ float2 update_mode(const LineParams& P, const LinePre
   return (has_chan && keep) ? c_scale(z, P.invN) : make_float2(0.f, 0.f);
 }
 
+// The turnaround of the CTA at tile (tx, ty), thread (tw, tm, tl) -- blockIdx.x/y and
+// threadIdx in a plain launch (turn_body); the batch member is blockIdx.z either way.
 template <int L, int NL, class Prog, class Spec = RtSpec>
-__device__ __forceinline__ void turn_body(const LineParams& P) {
+__device__ __forceinline__ void turn_body_at(const LineParams& P, int tx, int ty, int tw, int tm, int tl) {
   constexpr bool SP = Spec::kSplit;
   constexpr int R = LineCfg<L, SP>::R;
   constexpr bool Z3 = (NL == 2);   // the paired z-line form is the 3D turnaround
@@ -216,7 +218,7 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
     nk = NoiseKey{mk.key0, mk.key1, mk.step + P.step_off};
   }
   const Dims d = Spec::kSX ? Dims{Spec::kSX, Spec::kSY, Spec::kSZ} : dims_of(P);
-  const LineGeom<L, NL, Spec::kW, SP> g(P, d.sy, d.sx / 2);
+  const LineGeom<L, NL, Spec::kW, SP> g(P, d.sy, d.sx / 2, tx, ty, tw, tm, tl);
   if (g.idle) return;   // CTA-uniform, before any barrier
   const int m = g.m, l = g.l;
   const int slot_sz = g.slot_sz;
@@ -376,6 +378,11 @@ __device__ __forceinline__ void turn_body(const LineParams& P) {
   } else {
     for (int fi = 0; fi < nf; ++fi) field_step(fi);
   }
+}
+
+template <int L, int NL, class Prog, class Spec = RtSpec>
+__device__ __forceinline__ void turn_body(const LineParams& P) {
+  turn_body_at<L, NL, Prog, Spec>(P, blockIdx.x, blockIdx.y, threadIdx.x, threadIdx.y, threadIdx.z);
 }
 
 template <int L, int NL>

@@ -26,7 +26,7 @@ class ensemble {
   int addEquation(const std::string& equation);
   int addNoise(const std::string& field, const std::string& amplitude);
 
-  // A member: grid (powers of two), cell sizes, time step and noise seed.  Returns the
+  // A member: grid (2^a or 3*2^a per axis), cell sizes, time step and noise seed.  Returns the
   // member index.  Parameters not set per member keep their defaults.
   int addMember(int sx, int sy, int sz, float dx, float dy, float dz, float dt, unsigned long long seed);
   int setMemberParameter(int member, const std::string& name, float value);
@@ -35,7 +35,10 @@ class ensemble {
   // at zero; setReal gives initial conditions (sx*sy*sz floats, the evolver's layout).
   void prepare();
   int setReal(int member, const std::string& field, const float* host_real);
-  // nsteps time steps of every member (all groups concurrently); returns when done.
+  // nsteps time steps of every member; returns when done.  Members are grouped by grid
+  // (and cell size, time step); when every group is a 1D/2D grid of the same system
+  // structure (up to 8 groups), each kernel of a step is one launch over all groups
+  // (fused()), else the groups step concurrently on their own streams.
   int advance(int nsteps);
   int getReal(int member, const std::string& field, float* host_real);
 
@@ -43,7 +46,9 @@ class ensemble {
   int groups() const;
   long long deviceBytes() const;
   long long launches() const;
-  // JSON: one entry per group (grid, members, autotuned launch shapes).
+  bool fused() const;
+  // JSON {"groups": [per group: grid, members, autotuned launch shapes], "fused": the fused
+  // launches per grid class, or null with "why_not_fused"}.
   std::string describe() const;
 
  private:

@@ -206,6 +206,25 @@ long long cupssgb_solver_estimate_bytes(cupssgb_solver* s, int members);
 /* 1 when all work queued on the solver's stream has finished, 0 while it runs. */
 int cupssgb_solver_query(cupssgb_solver* s);
 
+/* Fused stepping of several batched solvers of one system structure on different 1D/2D
+ * grids (no counterpart in the reference): each kernel of a step is one launch over all
+ * of them (the turnaround and the row pass of every grid, specialised to it, in one
+ * generated kernel each), replayed from CUDA graphs.  Every member's trajectory is the
+ * one its own solver would compute.  The solvers keep their buffers and their set/get
+ * calls; cupssgb_multi_advance replaces cupssgb_solver_advance on them. */
+typedef struct cupssgb_multi cupssgb_multi;
+/* 0 when the solvers can be fused, else CUPSSGB_ERR_UNSUPPORTED with the reason in buf. */
+int cupssgb_multi_check(cupssgb_solver* const* solvers, int n, char* buf, int buflen);
+int cupssgb_multi_create(cupssgb_solver* const* solvers, int n, cupssgb_multi** out);
+int cupssgb_multi_destroy(cupssgb_multi* m);
+int cupssgb_multi_advance(cupssgb_multi* m, int nsteps);
+long long cupssgb_multi_launch_count(const cupssgb_multi* m);
+int cupssgb_multi_describe(const cupssgb_multi* m, char* buf, int buflen);
+/* Source of the fused kernels of phase 0 (non-dynamic fields) or 1 (dynamic fields) for
+ * these solvers, prepared or not (no GPU needed); returns its length ("" when the phase
+ * has no fields), or an error code as cupssgb_multi_check. */
+int cupssgb_multi_generated_source(cupssgb_solver* const* solvers, int n, int phase, char* buf, int buflen);
+
 /* ---------------- process helpers ---------------- */
 /* Page-locked host memory for the host-buffer entry points (cudaMallocHost). */
 int cupssgb_host_alloc(long long bytes, void** out);

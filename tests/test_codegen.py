@@ -126,3 +126,61 @@ def test_member_memory_estimate(built_lib):
         assert per >= 4 * 4 * npts
         assert s.estimate_bytes(1) > 0
         s.close()
+
+
+KPZ_IR = ([("h", 1), ("iqxh", 0), ("iqyh", 0)], {"nu": 1.0, "lam": 1.0, "D": 1.0},
+          ["dt h + nu*q^2*h = 0.5*lam*iqxh^2 + 0.5*lam*iqyh^2", "iqxh = iqx*h", "iqyh = iqy*h"],
+          [("h", "2*D")])
+CH_IR = ([("phi", 1)], {"a": -1.0, "b": 1.0, "k": 1.0, "T": 0.01},
+         ["dt phi + q^2*(a + k*q^2)*phi = -b*q^2*phi^3"], [("phi", "2*T*q^2")])
+
+
+def batched(ir, shape, members=4):
+    s = solver_from_ir(ir, shape)
+    s.set_members(members)
+    return s
+
+
+@pytest.mark.parametrize("system,shapes", [
+    ("kpz", [(32, 32, 1), (64, 64, 1), (128, 128, 1), (256, 256, 1), (512, 512, 1), (1024, 1024, 1)]),
+    ("kpz", [(64, 128, 1), (96, 96, 1), (384, 192, 1)]),
+    ("ch", [(64, 64, 1), (1024, 512, 1), (96, 192, 1), (256, 1, 1), (2048, 1024, 1)]),
+])
+def test_fused_kernels_compile(built_lib, system, shapes):
+    """The kernels that step several grid sizes in one launch per kernel (one body per
+    grid, selected by block range) compile for sm_103a: phase 1 (products) holds a fused
+    row pass and turnaround, phase 0 (KPZ's iqxh, iqyh) a fused turnaround."""
+    from cupss_gb300.api import jit_check, multi_generated_sources
+    from tests.test_parser_parity import build_lib
+    ir = build_lib(*(KPZ_IR if system == "kpz" else CH_IR))
+    solvers = [batched(ir, sh) for sh in shapes]
+    src0, src1 = multi_generated_sources(solvers)
+    assert bool(src0) == (system == "kpz")
+    assert "cupssgb_turn_multi" in src1 and "cupssgb_row_multi" in src1
+    for c in range(len(shapes)):
+        assert "MP.span[%d]" % c in src1
+    for src in (src0, src1):
+        if src:
+            assert jit_check(src) > 0
+    for s in solvers:
+        s.close()
+
+
+def test_fused_refusals(built_lib):
+    """3D grids, different systems, plain (unbatched) solvers and rows whose pass needs
+    another block shape are not fused (the ensemble then steps each grid on its own)."""
+    import cupss_gb300 as c
+    from cupss_gb300.api import multi_generated_sources
+    from tests.test_parser_parity import build_lib
+    kpz, ch = build_lib(*KPZ_IR), build_lib(*CH_IR)
+    cases = [([batched(ch, (32, 32, 1)), batched(ch, (16, 16, 16))], "1D and 2D"),
+             ([batched(ch, (32, 32, 1)), batched(kpz, (64, 64, 1))], "structure"),
+             ([batched(ch, (32, 32, 1)), solver_from_ir(ch, (64, 64, 1))], "batched"),
+             # rows of sx = 48 take a row-pass block other than the fused one's 128 threads
+             ([batched(ch, (48, 192, 1)), batched(ch, (64, 64, 1))], "row pass block")]
+    for solvers, why in cases:
+        with pytest.raises(c.CupssError) as ex:
+            multi_generated_sources(solvers)
+        assert why in str(ex.value), str(ex.value)
+        for s in solvers:
+            s.close()

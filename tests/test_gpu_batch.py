@@ -103,8 +103,10 @@ def test_ensemble_members_match_single_solves(nsteps):
         for nm in ("h", "iqxh", "iqyh"):
             err = rel(e.getReal(m, nm), ref[nm])
             assert err < 1e-6, (m, nm, err)
-    tune = e.describe()
-    assert len(tune) == 3 and all(g["tune"] for g in tune)
+    d = e.describe()
+    assert len(d["groups"]) == 3 and all(g["tune"] for g in d["groups"])
+    # three 2D grid sizes of one system: stepped by the fused launches
+    assert d["fused"] is not None, d
 
 
 def test_ensemble_3d_noisy_matches_single_solves():
@@ -241,3 +243,62 @@ def test_batch_trailing_inactive_members_are_not_launched():
     assert rel(s.get_real_member(f, 0), single(100, 48)) < 1e-6
     assert rel(s.get_real_member(f, 3), single(103, 16)) < 1e-6
     s.close()
+
+
+def launches_per_step(sizes, per_size=2, steps=32):
+    e = make_ensemble(KPZ)
+    k = 0
+    for side in sizes:
+        for _ in range(per_size):
+            e.addMember(side, side, 1, dt=0.005, seed=500 + k)
+            k += 1
+    e.prepare()
+    e.advance(16)   # the graphs are captured here
+    l0 = e.launch_count
+    e.advance(steps)
+    n = (e.launch_count - l0) / steps
+    d = e.describe()
+    e.close()
+    return n, d
+
+
+def test_fused_launches_do_not_grow_with_the_number_of_grid_sizes():
+    # KPZ: phase 0 (iqxh, iqyh) is one turnaround, phase 1 a row pass and a turnaround,
+    # and one step-count update per 16-step graph -- for one grid size (the solver's own
+    # graphs) as for four (the fused launches)
+    n1, d1 = launches_per_step([128])
+    n2, d2 = launches_per_step([64, 256])
+    n4, d4 = launches_per_step([64, 128, 256, 512])
+    assert d1["fused"] is None and d2["fused"] is not None and d4["fused"] is not None, (d1, d2, d4)
+    assert len(d4["fused"]["classes"]) == 4
+    assert d4["fused"]["launches_per_step"] == 3
+    assert n4 == n2 == 3 + 1 / 16, (n2, n4)
+    assert n4 <= n1, (n1, n4)
+
+
+def test_fused_off_by_environment(monkeypatch):
+    monkeypatch.setenv("CUPSSGB_FUSE", "0")
+    n4, d4 = launches_per_step([64, 128, 256, 512], steps=16)
+    assert d4["fused"] is None and d4["why_not_fused"] == "CUPSSGB_FUSE=0"
+    assert n4 > 4 * 3
+
+
+def test_fused_four_sizes_match_single_solves():
+    sizes = [64, 128, 256, 512]
+    e = make_ensemble(KPZ)
+    spec = []
+    for i, side in enumerate(sizes * 2):
+        vals = {"nu": 0.5 + 0.2 * i, "lam": 0.3 * i}
+        init = splitmix64_uniform(side * side, 70 + i, -0.2, 0.2).reshape(side, side)
+        e.addMember(side, side, 1, dt=0.005, seed=900 + i, **vals)
+        spec.append(((side, side, 1), vals, 900 + i, init))
+    e.prepare()
+    assert e.describe()["fused"] is not None
+    for m, (_, _, _, init) in enumerate(spec):
+        e.setReal(m, "h", init)
+    e.advance(21)
+    for m, (shape, vals, seed, init) in enumerate(spec):
+        ref = plain(KPZ, shape, 0.005, vals, seed, {"h": init}, 21)
+        for nm in ("h", "iqxh", "iqyh"):
+            err = rel(e.getReal(m, nm), ref[nm])
+            assert err < 1e-6, (m, shape, nm, err)

@@ -345,10 +345,13 @@ def bench_ensemble(args):
     pts = sum(m["side"] ** 2 for m in members)
 
     def run(fuse, sample_clocks):
-        # fuse=False: every grid size stepped by its own graphs on its own stream
+        # fuse "0": every grid size stepped by its own graphs on its own stream; "1": the
+        # fused launches; None: the form prepare times as faster
         old = os.environ.get("CUPSSGB_FUSE")
-        if not fuse:
-            os.environ["CUPSSGB_FUSE"] = "0"
+        if fuse is None:
+            os.environ.pop("CUPSSGB_FUSE", None)
+        else:
+            os.environ["CUPSSGB_FUSE"] = fuse
         try:
             t0 = time.perf_counter()
             ens = c.Ensemble()
@@ -377,15 +380,16 @@ def bench_ensemble(args):
         ens.close()
         return r
 
-    fused = run(True, True)
-    grouped = run(False, False)
-    t_ens, prep_s, launches, outs = fused["seconds"], fused["prepare_seconds"], fused["launches"], fused["outs"]
-    clk, groups, dev_bytes = fused["clocks"], fused["describe"], fused["device_bytes"]
+    chosen = run(None, True)
+    forms = {"fused": run("1", False), "grouped": run("0", False)}
+    t_ens, prep_s, launches, outs = chosen["seconds"], chosen["prepare_seconds"], chosen["launches"], chosen["outs"]
+    clk, groups, dev_bytes = chosen["clocks"], chosen["describe"], chosen["device_bytes"]
     finite = [bool(np.isfinite(o).all()) for o in outs]
-    # the fused and grouped forms run the same arithmetic per member
-    fg_worst = max((float(np.linalg.norm(a.astype(np.float64) - b) / max(np.linalg.norm(b), 1e-30))
-                    for a, b in zip(outs, grouped["outs"]) if np.isfinite(a).all() and np.isfinite(b).all()),
-                   default=0.0)
+
+    def worst_vs_chosen(r):
+        # both forms run the same arithmetic per member
+        return max((float(np.linalg.norm(a.astype(np.float64) - b) / max(np.linalg.norm(b), 1e-30))
+                    for a, b in zip(r["outs"], outs) if np.isfinite(a).all() and np.isfinite(b).all()), default=0.0)
 
     # the same solves with the plain evolver, one after another
     nplain = n if args.plain_members is None else min(n, args.plain_members)
@@ -441,11 +445,13 @@ def bench_ensemble(args):
                                  "members_run": nplain, "pt_steps_per_s": pts_plain * steps / t_plain},
             "speedup_vs_plain": t_plain_all / t_ens, "seconds": t_ens, "prepare_seconds": prep_s,
             "gpu_launches": launches, "clocks": clk,
-            "fused": groups.get("fused") is not None,
-            "grouped": {"value": n / grouped["seconds"], "unit": "solves/s", "seconds": grouped["seconds"],
-                        "gpu_launches": grouped["launches"], "prepare_seconds": grouped["prepare_seconds"],
-                        "worst_rel_l2_vs_fused": fg_worst,
-                        "what": "the same ensemble with CUPSSGB_FUSE=0: each grid size's own graphs on its own stream"},
+            "form": (groups.get("fused") or {}).get("form", "grouped"),
+            "forms": {k: {"value": n / r["seconds"], "unit": "solves/s", "seconds": r["seconds"],
+                          "gpu_launches": r["launches"], "worst_rel_l2_vs_chosen": worst_vs_chosen(r)}
+                      for k, r in forms.items()},
+            "forms_what": "the same ensemble forced into each form (CUPSSGB_FUSE=1: one launch per kernel "
+                          "over every grid size; =0: each grid size's own graphs on its own stream); the "
+                          "line's value is the form prepare timed as faster",
             "accuracy": {"finite_members": int(sum(finite)), "members_compared": nplain,
                          "members_equal_to_plain": int(agree), "worst_rel_l2_vs_plain": worst,
                          "note": "members that diverge (large lambda^2 D / nu^3) do so identically in the plain "

@@ -474,6 +474,14 @@ int cupssgb_multi_describe(const cupssgb_multi* m, char* buf, int buflen) {
   return copy_out(m->m->describe(), buf, buflen);
 }
 
+int cupssgb_multi_choose(cupssgb_multi* m) {
+  NEED(m);
+  return guard([&] {
+    m->m->choose();
+    return m->m->fused() ? 1 : 0;
+  });
+}
+
 int cupssgb_multi_generated_source(cupssgb_solver* const* solvers, int n, int phase, char* buf, int buflen) {
   std::string src;
   const int rc = guard([&] {

@@ -8,6 +8,7 @@
 #include "fft.cuh"
 #include "jit.h"
 #include "launch.h"
+#include "tune_cache.h"
 
 namespace cupssgb {
 
@@ -171,6 +172,7 @@ void MultiStep::build() {
     const std::string why = plan_phase(s_, ph, K, &src);
     if (!why.empty()) throw Error(kErrUnsupported, why);
     if (!K.active) continue;
+    src_hash_ = fnv1a64(std::to_string(src_hash_) + src);
     K.turn = jit_kernel(src, "cupssgb_turn_multi");
     if (K.has_row) K.row = jit_kernel(src, "cupssgb_row_multi");
   }
@@ -273,6 +275,11 @@ void MultiStep::capture(int c, int parity) {
 
 void MultiStep::advance(int nsteps) {
   if (nsteps < 0) throw Error(kErrInvalid, "nsteps < 0");
+  if (!fused_) {
+    // each class on its own stream, concurrently
+    for (Solver* S : s_) S->advance(nsteps);
+    return;
+  }
   for (Solver* S : s_)
     if (S->mvals_dirty_) S->upload_member_values();
   const int parity = s_[0]->par_.empty() ? 0 : s_[0]->par_[0];
@@ -314,6 +321,95 @@ void MultiStep::advance(int nsteps) {
   for (Solver* S : s_) check(cudaStreamWaitEvent(S->stream_, ev_, 0), "cudaStreamWaitEvent");
 }
 
+void MultiStep::restart() {
+  for (Solver* S : s_) {
+    S->zero_dynamic_buffers();
+    for (MemberK& k : S->members_h_) k.step = 0u;
+    check(cudaMemcpyAsync(S->members_d_, S->members_h_.data(), S->members_h_.size() * sizeof(MemberK),
+                          cudaMemcpyHostToDevice, S->stream_),
+          "member upload");
+    S->step_ = 0;
+    check(cudaStreamSynchronize(S->stream_), "restart");
+  }
+}
+
+std::string MultiStep::choice_key() const {
+  int dev = 0;
+  check(cudaGetDevice(&dev), "cudaGetDevice");
+  cudaDeviceProp pr;
+  check(cudaGetDeviceProperties(&pr, dev), "cudaGetDeviceProperties");
+  std::string gpu = pr.name;
+  for (char& ch : gpu)
+    if (ch == ' ' || ch == '\t' || ch == '/') ch = '_';
+  std::ostringstream os;
+  os << "multi1/" << gpu << "/sm" << pr.multiProcessorCount << "/";
+  for (const Solver* S : s_) os << S->sx_ << "x" << S->sy_ << "x" << S->sz_ << "m" << S->mspan_ << ",";
+  char h[17];
+  std::snprintf(h, sizeof(h), "%016llx", (unsigned long long)src_hash_);
+  os << "/" << h;
+  return os.str();
+}
+
+void MultiStep::choose() {
+  chosen_ = true;
+  const std::string key = choice_key();
+  std::string cached;
+  double f = -1.0;
+  if (tune_cache_lookup(key, &cached) && tune_value_get(cached, "fused", &f) && (f == 0.0 || f == 1.0) &&
+      tune_value_get(cached, "ms_fused", &ms_fused_) && tune_value_get(cached, "ms_grouped", &ms_grouped_)) {
+    fused_ = f == 1.0;
+    choice_cached_ = true;
+    return;
+  }
+  constexpr int kSteps = 16;
+  const long long l0 = launches_;
+  std::vector<long long> sl0;
+  for (Solver* S : s_) sl0.push_back(S->launches_);
+  cudaEvent_t a = nullptr, b = nullptr;
+  check(cudaEventCreate(&a), "cudaEventCreate");
+  check(cudaEventCreate(&b), "cudaEventCreate");
+  auto timed = [&](bool fused) {
+    fused_ = fused;
+    advance(kSteps);   // warm-up: graphs captured
+    check(cudaStreamSynchronize(stream_), "choose");
+    for (Solver* S : s_) check(cudaStreamSynchronize(S->stream_), "choose");
+    check(cudaEventRecord(a, stream_), "cudaEventRecord");
+    for (Solver* S : s_) check(cudaStreamWaitEvent(S->stream_, a, 0), "cudaStreamWaitEvent");
+    if (fused) {
+      advance(kSteps);   // waits on the class streams, which wait on a
+    } else {
+      advance(kSteps);
+      for (size_t c = 0; c < s_.size(); ++c) {
+        check(cudaEventRecord(class_ev_[c], s_[c]->stream_), "cudaEventRecord");
+        check(cudaStreamWaitEvent(stream_, class_ev_[c], 0), "cudaStreamWaitEvent");
+      }
+    }
+    check(cudaEventRecord(b, stream_), "cudaEventRecord");
+    check(cudaEventSynchronize(b), "cudaEventSynchronize");
+    float ms = 0.f;
+    check(cudaEventElapsedTime(&ms, a, b), "cudaEventElapsedTime");
+    return (double)ms / kSteps;
+  };
+  try {
+    ms_fused_ = timed(true);
+    ms_grouped_ = timed(false);
+  } catch (...) {
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    fused_ = true;
+    throw;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  fused_ = ms_fused_ <= ms_grouped_;
+  launches_ = l0;
+  for (size_t c = 0; c < s_.size(); ++c) s_[c]->launches_ = sl0[c];
+  restart();
+  std::ostringstream v;
+  v << "fused=" << (fused_ ? 1 : 0) << " ms_fused=" << ms_fused_ << " ms_grouped=" << ms_grouped_;
+  tune_cache_store(key, v.str());
+}
+
 std::string MultiStep::describe() const {
   std::ostringstream os;
   os << "{\"classes\": [";
@@ -332,7 +428,11 @@ std::string MultiStep::describe() const {
     os << "}";
   }
   os << "], \"launches_per_step\": " << ((ph_[0].active ? 1 + ph_[0].has_row : 0) + (ph_[1].active ? 1 + ph_[1].has_row : 0))
-     << "}";
+     << ", \"form\": \"" << (fused_ ? "fused" : "grouped") << "\"";
+  if (chosen_)
+    os << ", \"ms_per_step\": {\"fused\": " << ms_fused_ << ", \"grouped\": " << ms_grouped_
+       << "}, \"cached\": " << (choice_cached_ ? "true" : "false");
+  os << "}";
   return os.str();
 }
 

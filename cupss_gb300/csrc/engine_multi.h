@@ -33,7 +33,15 @@ class MultiStep {
   MultiStep& operator=(const MultiStep&) = delete;
   void advance(int nsteps);
   long long launches() const { return launches_; }
-  std::string describe() const;   // JSON: per class grid, tile width, CTAs
+  std::string describe() const;   // JSON: per class grid, tile width, CTAs; the form chosen
+  // Times the fused launches against every class stepping alone on its own stream
+  // (their own tuned graphs, running concurrently), 16 steps each after 16 warm-up steps,
+  // on the solvers' current buffers, and steps with the faster form from then on.  The
+  // buffers are zeroed and every member is back at step 0 afterwards, as after prepare,
+  // so call it before setting fields.  The choice is cached in the tune cache (key: GPU,
+  // grids, member spans, kernel sources) and taken from there the next time.
+  void choose();
+  bool fused() const { return fused_; }
 
  private:
   struct PhaseK {
@@ -47,14 +55,21 @@ class MultiStep {
   // Launch shapes of phase ph and (src != nullptr) the source of its fused kernels;
   // "" when every class fits them, else the reason.
   static std::string plan_phase(const std::vector<Solver*>& s, int ph, PhaseK& K, std::string* src);
-  void check(cudaError_t e, const char* what);
+  static void check(cudaError_t e, const char* what);
   void build();
   void launch_phase(int ph, uint32_t off);
   void step_once(uint32_t off, bool tick);
   void capture(int c, int parity);
 
+  void restart();   // zero buffers, members at step 0 (after timing)
+  std::string choice_key() const;
+
   std::vector<Solver*> s_;
   PhaseK ph_[2];
+  uint64_t src_hash_ = 0;   // of the fused kernels' sources
+  bool fused_ = true;       // false: every class steps on its own stream
+  bool choice_cached_ = false, chosen_ = false;
+  double ms_fused_ = -1.0, ms_grouped_ = -1.0;   // per step, from choose()
   cudaStream_t stream_ = nullptr;
   cudaEvent_t ev_ = nullptr;
   std::vector<cudaEvent_t> class_ev_;

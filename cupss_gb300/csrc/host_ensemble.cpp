@@ -39,6 +39,7 @@ struct ensemble::Impl {
   // null when the groups do not qualify or CUPSSGB_FUSE=0
   cupssgb_multi* multi = nullptr;
   std::string multi_why;
+  bool multi_fused = false;   // the multi stepper runs the fused launches (else each group alone)
 
   int field_index(const std::string& name) const {
     for (size_t i = 0; i < fields.size(); ++i)
@@ -155,17 +156,27 @@ void ensemble::prepare() {
     ok(cupssgb_solver_prepare(g.solver));
   }
   // one launch per kernel and step across every grid size, where the groups allow it
-  const char* fuse = std::getenv("CUPSSGB_FUSE");
+  // (CUPSSGB_FUSE=1: always fused; =0: never; unset: the faster form, timed here on the
+  // zeroed buffers of the fresh groups)
+  const char* fe = std::getenv("CUPSSGB_FUSE");
+  const std::string fuse = fe ? fe : "";
   if (I.groups.size() < 2) {
     I.multi_why = "one grid class: stepped by its own tuned graphs";
-  } else if (!(fuse && std::string(fuse) == "0")) {
+  } else if (fuse != "0") {
     std::vector<cupssgb_solver*> sv;
     for (Impl::Group& g : I.groups) sv.push_back(g.solver);
     char why[256] = {0};
-    if (cupssgb_multi_check(sv.data(), (int)sv.size(), why, (int)sizeof(why)) == 0)
+    if (cupssgb_multi_check(sv.data(), (int)sv.size(), why, (int)sizeof(why)) == 0) {
       ok(cupssgb_multi_create(sv.data(), (int)sv.size(), &I.multi));
-    else
+      I.multi_fused = true;
+      if (fuse != "1") {
+        const int rc = cupssgb_multi_choose(I.multi);
+        ok(rc);
+        I.multi_fused = rc == 1;
+      }
+    } else {
       I.multi_why = why;
+    }
   } else {
     I.multi_why = "CUPSSGB_FUSE=0";
   }
@@ -218,7 +229,7 @@ long long ensemble::launches() const {
   return n;
 }
 
-bool ensemble::fused() const { return impl_->multi != nullptr; }
+bool ensemble::fused() const { return impl_->multi != nullptr && impl_->multi_fused; }
 
 std::string ensemble::describe() const {
   std::ostringstream os;

@@ -36,9 +36,10 @@ class ensemble {
   void prepare();
   int setReal(int member, const std::string& field, const float* host_real);
   // nsteps time steps of every member; returns when done.  Members are grouped by grid
-  // (and cell size, time step); when every group is a 1D/2D grid of the same system
-  // structure (up to 8 groups), each kernel of a step is one launch over all groups
-  // (fused()), else the groups step concurrently on their own streams.
+  // (and cell size, time step); the groups step concurrently on their own streams, or,
+  // when every group is a 1D/2D grid of the same system structure (up to 8 groups), each
+  // kernel of a step may be one launch over all groups (fused()).  prepare times both
+  // forms and keeps the faster (CUPSSGB_FUSE=1 / 0 forces fused / separate).
   int advance(int nsteps);
   int getReal(int member, const std::string& field, float* host_real);
 
@@ -48,7 +49,8 @@ class ensemble {
   long long launches() const;
   bool fused() const;
   // JSON {"groups": [per group: grid, members, autotuned launch shapes], "fused": the fused
-  // launches per grid class, or null with "why_not_fused"}.
+  // launches per grid class, the form chosen and both forms' ms per step, or null with
+  // "why_not_fused"}.
   std::string describe() const;
 
  private:

@@ -220,6 +220,12 @@ int cupssgb_multi_destroy(cupssgb_multi* m);
 int cupssgb_multi_advance(cupssgb_multi* m, int nsteps);
 long long cupssgb_multi_launch_count(const cupssgb_multi* m);
 int cupssgb_multi_describe(const cupssgb_multi* m, char* buf, int buflen);
+/* Times the fused launches against each solver stepping alone on its own stream (16 steps
+ * each after 16 warm-up steps) and steps with the faster form from then on.  Zeroes every
+ * field and puts every member back at step 0 afterwards, as after prepare: call it before
+ * setting fields.  The choice is cached with the autotuner's.  Returns 1 (fused) or 0
+ * (each solver on its own), or an error code. */
+int cupssgb_multi_choose(cupssgb_multi* m);
 /* Source of the fused kernels of phase 0 (non-dynamic fields) or 1 (dynamic fields) for
  * these solvers, prepared or not (no GPU needed); returns its length ("" when the phase
  * has no fields), or an error code as cupssgb_multi_check. */

@@ -246,7 +246,7 @@ def test_batch_trailing_inactive_members_are_not_launched():
 
 
 def launches_per_step(sizes, per_size=2, steps=32):
-    e = make_ensemble(KPZ)
+    e = make_ensemble(KPZ)   # CUPSSGB_FUSE=1 set by the caller: the fused form, untimed
     k = 0
     for side in sizes:
         for _ in range(per_size):
@@ -262,15 +262,16 @@ def launches_per_step(sizes, per_size=2, steps=32):
     return n, d
 
 
-def test_fused_launches_do_not_grow_with_the_number_of_grid_sizes():
+def test_fused_launches_do_not_grow_with_the_number_of_grid_sizes(monkeypatch):
     # KPZ: phase 0 (iqxh, iqyh) is one turnaround, phase 1 a row pass and a turnaround,
     # and one step-count update per 16-step graph -- for one grid size (the solver's own
     # graphs) as for four (the fused launches)
+    monkeypatch.setenv("CUPSSGB_FUSE", "1")
     n1, d1 = launches_per_step([128])
     n2, d2 = launches_per_step([64, 256])
     n4, d4 = launches_per_step([64, 128, 256, 512])
     assert d1["fused"] is None and d2["fused"] is not None and d4["fused"] is not None, (d1, d2, d4)
-    assert len(d4["fused"]["classes"]) == 4
+    assert len(d4["fused"]["classes"]) == 4 and d4["fused"]["form"] == "fused"
     assert d4["fused"]["launches_per_step"] == 3
     assert n4 == n2 == 3 + 1 / 16, (n2, n4)
     assert n4 <= n1, (n1, n4)
@@ -283,7 +284,15 @@ def test_fused_off_by_environment(monkeypatch):
     assert n4 > 4 * 3
 
 
-def test_fused_four_sizes_match_single_solves():
+@pytest.mark.parametrize("fuse", ["1", None])
+def test_fused_four_sizes_match_single_solves(monkeypatch, tmp_path, fuse):
+    """Forced fused form, and the timed choice (which steps both forms on the fresh
+    buffers and restarts them): either way every member equals its single solve."""
+    if fuse:
+        monkeypatch.setenv("CUPSSGB_FUSE", fuse)
+    else:
+        monkeypatch.delenv("CUPSSGB_FUSE", raising=False)
+        monkeypatch.setenv("CUPSSGB_TUNE_CACHE", str(tmp_path / "tune.txt"))   # timed, not cached
     sizes = [64, 128, 256, 512]
     e = make_ensemble(KPZ)
     spec = []
@@ -293,7 +302,12 @@ def test_fused_four_sizes_match_single_solves():
         e.addMember(side, side, 1, dt=0.005, seed=900 + i, **vals)
         spec.append(((side, side, 1), vals, 900 + i, init))
     e.prepare()
-    assert e.describe()["fused"] is not None
+    f = e.describe()["fused"]
+    assert f is not None
+    if fuse is None:
+        assert not f["cached"] and f["ms_per_step"]["fused"] > 0 and f["ms_per_step"]["grouped"] > 0
+        assert f["form"] == ("fused" if f["ms_per_step"]["fused"] <= f["ms_per_step"]["grouped"] else "grouped")
+        assert "multi1/" in (tmp_path / "tune.txt").read_text()
     for m, (_, _, _, init) in enumerate(spec):
         e.setReal(m, "h", init)
     e.advance(21)

@@ -124,6 +124,11 @@ class Solver:
     def get_real_ptr(self, f, host_ptr):
         capi.check(self.lib.cupssgb_solver_get_real(self.h, f, C.cast(host_ptr, capi._FP)))
 
+    def snapshot_real_ptr(self, f, host_ptr, done_event=None):
+        """Asynchronous read-out of field f into host memory (complete after synchronize
+        or once done_event, a cudaEvent_t handle, has been reached)."""
+        capi.check(self.lib.cupssgb_solver_snapshot_real(self.h, f, C.cast(host_ptr, C.c_void_p), done_event))
+
     # ---- batches ----
     def set_members(self, n):
         capi.check(self.lib.cupssgb_solver_set_members(self.h, int(n)))

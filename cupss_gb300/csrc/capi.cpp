@@ -198,8 +198,9 @@ int cupssgb_solver_set_real(cupssgb_solver* s, int field, const float* host_real
   NEED(s);
   NEED(host_real);
   return guard([&] {
-    s->s->set_real(field, host_real, false);
-    s->s->synchronize();
+    // a pageable source is copied before this returns (and errors surface here); a
+    // page-locked one stays in flight on the input stream
+    if (!s->s->set_real(field, host_real, false)) s->s->synchronize();
     return 0;
   });
 }
@@ -902,8 +903,7 @@ int cupssgb_solver_set_real_member(cupssgb_solver* s, int field, int member, con
   NEED(s);
   NEED(host_real);
   return guard([&] {
-    s->s->set_real(field, host_real, false, member);
-    s->s->synchronize();
+    if (!s->s->set_real(field, host_real, false, member)) s->s->synchronize();
     return 0;
   });
 }

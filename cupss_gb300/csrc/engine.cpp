@@ -60,6 +60,12 @@ Solver::~Solver() {
   for (cudaEvent_t e : out_free_)
     if (e) cudaEventDestroy(e);
   if (out_stream_) cudaStreamDestroy(out_stream_);
+  if (up_stream_) cudaStreamSynchronize(up_stream_);
+  for (int b = 0; b < 2; ++b) {
+    if (up_ready_[b]) cudaEventDestroy(up_ready_[b]);
+    if (up_free_[b]) cudaEventDestroy(up_free_[b]);
+  }
+  if (up_stream_) cudaStreamDestroy(up_stream_);
   for (auto& row : graph_)
     for (cudaGraphExec_t& g : row)
       if (g) cudaGraphExecDestroy(g);
@@ -372,14 +378,52 @@ void Solver::line_fwd_inv(int geo, int mode, const float2* in, float2* out, int 
   ++launches_;
 }
 
-void Solver::set_real(int f, const float* src, bool on_device, int m) {
+// Page-locked host memory (cudaMallocHost / cudaHostAlloc / cudaHostRegister) is mapped
+// into the device's address space: get_real's row pass writes the field to it directly
+// over the host link (about 10% faster than a copy out of device memory for a 64 MiB field
+// on a GB300), and set_real copies from it asynchronously on an input stream.  nullptr for
+// pageable memory, an address not 16-byte aligned, or CUPSSGB_HOST_DIRECT=0.
+static void* host_direct(const void* p) {
+  const char* e = std::getenv("CUPSSGB_HOST_DIRECT");
+  if ((e && std::string(e) == "0") || !p || (reinterpret_cast<uintptr_t>(p) & 15u) != 0) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+  return (reinterpret_cast<uintptr_t>(a.devicePointer) & 15u) == 0 ? a.devicePointer : nullptr;
+}
+
+bool Solver::set_real(int f, const float* src, bool on_device, int m) {
   if (!prepared_) throw Error(kErrState, "set_real before prepare");
   if (f < 0 || f >= nfields()) throw Error(kErrInvalid, "bad field index");
   check_member(m);
   const size_t n = npoints();
-  check(cudaMemcpyAsync(scratch_real_, src, n * sizeof(float),
-                        on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream_),
-        "set_real copy");
+  const float* in = scratch_real_;
+  int b = -1;
+  if (!on_device && host_direct(src)) {
+    // page-locked source: copied on the input stream into a staging buffer, so that the
+    // copy overlaps what the solver stream still runs (the previous step, its output)
+    if (!up_stream_) check(cudaStreamCreateWithFlags(&up_stream_, cudaStreamNonBlocking), "input stream");
+    b = up_next_;
+    up_next_ ^= 1;
+    if (!up_stage_[b]) {
+      up_stage_[b] = (float*)dalloc(n * sizeof(float));
+      check(cudaEventCreateWithFlags(&up_ready_[b], cudaEventDisableTiming), "cudaEventCreate");
+      check(cudaEventCreateWithFlags(&up_free_[b], cudaEventDisableTiming), "cudaEventCreate");
+    } else {
+      check(cudaStreamWaitEvent(up_stream_, up_free_[b], 0), "cudaStreamWaitEvent");
+    }
+    check(cudaMemcpyAsync(up_stage_[b], src, n * sizeof(float), cudaMemcpyHostToDevice, up_stream_), "set_real copy");
+    check(cudaEventRecord(up_ready_[b], up_stream_), "cudaEventRecord");
+    check(cudaStreamWaitEvent(stream_, up_ready_[b], 0), "cudaStreamWaitEvent");
+    in = up_stage_[b];
+  } else {
+    check(cudaMemcpyAsync(scratch_real_, src, n * sizeof(float),
+                          on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream_),
+          "set_real copy");
+  }
   float2* st = state_[par_[f]][f] + (size_t)m * half_;
   XParams x;
   std::memset(&x, 0, sizeof(x));
@@ -389,7 +433,7 @@ void Solver::set_real(int f, const float* src, bool on_device, int m) {
   x.out_mode = kXOutSpectral;
   x.out_scale = 1.f;
   x.n_in = 1;
-  x.in[0] = reinterpret_cast<const float2*>(scratch_real_);
+  x.in[0] = reinterpret_cast<const float2*>(in);
   x.n_prod = 1;
   x.out[0] = st;
   x.prod_n[0] = 1;
@@ -397,12 +441,14 @@ void Solver::set_real(int f, const float* src, bool on_device, int m) {
   x.tw = tw_;
   check(launch_row_pass(x, stream_), "row pass (upload)");
   ++launches_;
+  if (b >= 0) check(cudaEventRecord(up_free_[b], stream_), "cudaEventRecord");
   if (dim_ == 3) {
     line_fwd_inv(kGeoY3, kModeFwd, st, st, Lx_);
     line_fwd_inv(kGeoZ3, kModeFwd, st, st, Lx_);
   } else if (sy_ > 1) {
     line_fwd_inv(kGeoCol, kModeFwd, st, st, Lx_);
   }
+  return b >= 0;
 }
 
 void Solver::to_real_scratch(int f, int m, float* dst) {
@@ -440,24 +486,29 @@ void Solver::snapshot_real(int f, float* host_dst, cudaEvent_t done) {
   if (!host_dst) throw Error(kErrInvalid, "null host buffer");
   if (!out_stream_) {
     check(cudaStreamCreateWithFlags(&out_stream_, cudaStreamNonBlocking), "output stream");
-    out_stage_.assign(nfields(), nullptr);
-    out_ready_.assign(nfields(), nullptr);
-    out_free_.assign(nfields(), nullptr);
+    out_stage_.assign(2 * nfields(), nullptr);
+    out_ready_.assign(2 * nfields(), nullptr);
+    out_free_.assign(2 * nfields(), nullptr);
+    out_next_.assign(nfields(), 0);
   }
-  if (!out_stage_[f]) {
-    out_stage_[f] = (float*)dalloc(npoints() * sizeof(float));
-    check(cudaEventCreateWithFlags(&out_ready_[f], cudaEventDisableTiming), "cudaEventCreate");
-    check(cudaEventCreateWithFlags(&out_free_[f], cudaEventDisableTiming), "cudaEventCreate");
+  // two staging buffers per field, used in turn: the field of one snapshot is written
+  // while the copy of the previous one still runs
+  const int k = 2 * f + out_next_[f];
+  out_next_[f] ^= 1;
+  if (!out_stage_[k]) {
+    out_stage_[k] = (float*)dalloc(npoints() * sizeof(float));
+    check(cudaEventCreateWithFlags(&out_ready_[k], cudaEventDisableTiming), "cudaEventCreate");
+    check(cudaEventCreateWithFlags(&out_free_[k], cudaEventDisableTiming), "cudaEventCreate");
   } else {
-    // the previous copy of this field must have left the staging buffer
-    check(cudaStreamWaitEvent(stream_, out_free_[f], 0), "cudaStreamWaitEvent");
+    // the copy of this buffer's previous snapshot must have left it
+    check(cudaStreamWaitEvent(stream_, out_free_[k], 0), "cudaStreamWaitEvent");
   }
-  to_real_scratch(f, 0, out_stage_[f]);
-  check(cudaEventRecord(out_ready_[f], stream_), "cudaEventRecord");
-  check(cudaStreamWaitEvent(out_stream_, out_ready_[f], 0), "cudaStreamWaitEvent");
-  check(cudaMemcpyAsync(host_dst, out_stage_[f], npoints() * sizeof(float), cudaMemcpyDeviceToHost, out_stream_),
+  to_real_scratch(f, 0, out_stage_[k]);
+  check(cudaEventRecord(out_ready_[k], stream_), "cudaEventRecord");
+  check(cudaStreamWaitEvent(out_stream_, out_ready_[k], 0), "cudaStreamWaitEvent");
+  check(cudaMemcpyAsync(host_dst, out_stage_[k], npoints() * sizeof(float), cudaMemcpyDeviceToHost, out_stream_),
         "snapshot copy");
-  check(cudaEventRecord(out_free_[f], out_stream_), "cudaEventRecord");
+  check(cudaEventRecord(out_free_[k], out_stream_), "cudaEventRecord");
   if (done) check(cudaEventRecord(done, out_stream_), "cudaEventRecord");
 }
 
@@ -465,6 +516,11 @@ void Solver::get_real(int f, float* dst, bool on_device, int m) {
   if (!prepared_) throw Error(kErrState, "get_real before prepare");
   if (f < 0 || f >= nfields()) throw Error(kErrInvalid, "bad field index");
   check_member(m);
+  if (float* d = on_device ? nullptr : static_cast<float*>(host_direct(dst))) {
+    to_real_scratch(f, m, d);   // the row pass stores the field in host memory
+    check(cudaStreamSynchronize(stream_), "get_real sync");
+    return;
+  }
   to_real_scratch(f, m);
   check(cudaMemcpyAsync(dst, scratch_real_, npoints() * sizeof(float),
                         on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, stream_),
@@ -685,7 +741,9 @@ void Solver::get_fourier(int f, float2* dst, bool on_device, int m) {
 }
 
 void Solver::synchronize() {
+  if (up_stream_) check(cudaStreamSynchronize(up_stream_), "synchronize");
   if (stream_) check(cudaStreamSynchronize(stream_), "synchronize");
+  if (out_stream_) check(cudaStreamSynchronize(out_stream_), "synchronize");
 }
 
 void Solver::fill_turn(const Phase& P, LineParams& p, int& nslots, bool& any_chan,

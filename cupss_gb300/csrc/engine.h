@@ -69,8 +69,9 @@ class Solver {
 
   void prepare();
   bool prepared() const { return prepared_; }
-  // m: batch member (0 for a single system)
-  void set_real(int f, const float* src, bool src_on_device, int m = 0);
+  // m: batch member (0 for a single system).  Returns true when the copy of a host
+  // source runs asynchronously (page-locked memory, input stream), false otherwise.
+  bool set_real(int f, const float* src, bool src_on_device, int m = 0);
   void advance(int nsteps);
   void get_real(int f, float* dst, bool dst_on_device, int m = 0);
   void get_fourier(int f, float2* dst, bool dst_on_device, int m = 0);
@@ -79,8 +80,8 @@ class Solver {
   // materialised on the solver's stream into a device staging buffer of its own; the
   // device-to-host copy then runs on a separate output stream, and `done` (if not null) is
   // recorded there once the host copy is complete.  host_dst should be page-locked for the
-  // copy to be asynchronous.  A later snapshot of the same field first waits until the
-  // previous copy has left its staging buffer.
+  // copy to be asynchronous.  Each field has two staging buffers, used in turn; a snapshot
+  // first waits until the copy of the one before the previous has left its buffer.
   void snapshot_real(int f, float* host_dst, cudaEvent_t done);
 
   // ---- batches: n independent systems of this structure and grid in one solver ----
@@ -262,9 +263,18 @@ class Solver {
   float2* scratch_full_ = nullptr;   // reference-layout full spectrum, allocated on first use
   // output path (snapshot_real), created on first use
   cudaStream_t out_stream_ = nullptr;
-  std::vector<float*> out_stage_;          // per field: staging copy of the real values
-  std::vector<cudaEvent_t> out_ready_;     // per field: staging copy written (solver stream)
-  std::vector<cudaEvent_t> out_free_;      // per field: staging copy read out (output stream)
+  std::vector<float*> out_stage_;          // per field, two: staging copies of the real values
+  std::vector<cudaEvent_t> out_ready_;     // per staging buffer: written (solver stream)
+  std::vector<cudaEvent_t> out_free_;      // per staging buffer: read out (output stream)
+  std::vector<int> out_next_;              // per field: the staging buffer of its next snapshot
+  // input path (set_real from page-locked host memory), created on first use: the copy
+  // runs on its own stream into one of two staging buffers, so that it overlaps the
+  // solver stream's work queued before it
+  cudaStream_t up_stream_ = nullptr;
+  float* up_stage_[2] = {nullptr, nullptr};
+  cudaEvent_t up_ready_[2] = {nullptr, nullptr};   // staging copy written (input stream)
+  cudaEvent_t up_free_[2] = {nullptr, nullptr};    // staging copy read (solver stream)
+  int up_next_ = 0;
   std::vector<void*> allocs_;
   Phase phases_[2];              // 0: non-dynamic, 1: dynamic
   // kernel timing

@@ -92,7 +92,10 @@ int cupssgb_solver_set_seed(cupssgb_solver* s, unsigned long long seed);
  * plan and allocates device state.  All fields start at zero. */
 int cupssgb_solver_prepare(cupssgb_solver* s);
 /* Initial condition: copyHostToDevice + toComp of evolver::prepareProblem
- * (src/evolver.cpp:114-117).  host_real: sx*sy*sz floats. */
+ * (src/evolver.cpp:114-117).  host_real: sx*sy*sz floats.  From page-locked memory
+ * (cupssgb_host_alloc) the copy is asynchronous, on an input stream of its own that
+ * overlaps work queued earlier (host_real must stay unchanged until the solver's next
+ * synchronising call); from pageable memory it completes before the call returns. */
 int cupssgb_solver_set_real(cupssgb_solver* s, int field, const float* host_real);
 /* Same from a device pointer (stream-ordered on the solver's stream). */
 int cupssgb_solver_set_real_device(cupssgb_solver* s, int field, const float* dev_real);
@@ -121,16 +124,18 @@ int cupssgb_solver_get_dealiased_pairs_device(cupssgb_solver* s, int field, floa
 int cupssgb_solver_set_fourier_device(cupssgb_solver* s, int field, const float* dev_complex);
 int cupssgb_solver_set_real_pairs_device(cupssgb_solver* s, int field, const float* dev_pairs,
                                          const float* dev_dealiased_pairs);
-/* Waits for all work queued on the solver's stream. */
+/* Waits for all work queued on the solver: its stream, and the input copies and output
+ * copies (cupssgb_solver_snapshot_real) on their own streams. */
 int cupssgb_solver_synchronize(cupssgb_solver* s);
 /* Output path of writeOut (src/field.cpp:350-402): copies the real values of a field into
  * host memory without stalling the step.  The field is materialised on the solver's
- * stream into a staging buffer of its own (allocated on the first call for that field);
+ * stream into a staging buffer of its own (allocated on first use);
  * the device-to-host copy runs on a separate output stream, so steps queued after this
  * call overlap with it.  done_event (a cudaEvent_t, may be NULL) is recorded on the
  * output stream once host_real holds the values; host_real should be page-locked
- * (cupssgb_host_alloc) for the copy to be asynchronous.  A later snapshot of the same
- * field waits until the previous copy has left the staging buffer. */
+ * (cupssgb_host_alloc) for the copy to be asynchronous.  Each field has two staging
+ * buffers, used in turn, so that a snapshot's transform overlaps the previous snapshot's
+ * copy; a snapshot waits until the copy two snapshots back has left its buffer. */
 int cupssgb_solver_snapshot_real(cupssgb_solver* s, int field, float* host_real, void* done_event);
 /* Steps taken so far, kernels launched so far, device bytes held. */
 long long cupssgb_solver_step_count(const cupssgb_solver* s);

@@ -15,7 +15,8 @@ namespace cupssgb {
 // turnaround and row pass are generated per set of classes (jit_generate_multi): each
 // class's body is specialised to its grid, owns a contiguous range of blockIdx.x and sees
 // its own members at blockIdx.z, so per-member data and noise are exactly those of the
-// class's own launches -- a member's trajectory is the one it has in its own solver.
+// class's own launches: a member's trajectory is the one it has in its own solver, to
+// rounding (the fused row pass is compiled by NVRTC, the solver's own by nvcc).
 // Steps are replayed from CUDA graphs of 16, 4 and 1 steps.  The classes keep their
 // buffers, member tables and set/get calls; stepping runs on this object's stream, which
 // waits for the classes' streams before each advance (and they for it after).

@@ -97,11 +97,6 @@ __device__ __forceinline__ void cp_async8(unsigned sa, const float2* gsrc, int s
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
-// Waits until at most N of this thread's committed copy groups are still in flight.
-template <int N>
-__device__ __forceinline__ void cp_async_wait_group() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
 #endif
 
 // Butterfly sums on the paired FP32 pipe of sm_100+ (one f32x2 instruction per complex

@@ -1,19 +1,8 @@
 // Row-pass instantiations and dispatch by Lx = sx/2 (2^a up to 1024, 3 * 2^a up to 192).
-#include <algorithm>
-#include <cstdlib>
-#include <string>
-
 #include "kernels.cuh"
 #include "launch.h"
 
 namespace cupssgb {
-
-// CUPSSGB_ROW_PIPE=1: the single-product row pass in its persistent, software-pipelined
-// form (row_pass_one_pipe).
-static bool row_pipe_on() {
-  const char* e = std::getenv("CUPSSGB_ROW_PIPE");
-  return e && std::string(e) == "1";
-}
 
 // One spectral input raised to one spectral product (phi^n): the register-resident form.
 static bool row_is_one(const XParams& p) {
@@ -28,25 +17,6 @@ static cudaError_t launch_row_form(const XParams& p, cudaStream_t st, int nz, bo
   dim3 block(C::M, C::RW);
   dim3 grid((p.rows + C::RW - 1) / C::RW, 1, nz);
   if (row_is_one(p)) {
-    if (row_pipe_on()) {
-      // persistent form: as many CTAs as fit on the GPU at once, batches spread evenly
-      static std::atomic<unsigned long long> attr_pipe{0};
-      const size_t smem = 3 * (size_t)C::RW * C::PL * sizeof(float2);
-      cudaError_t e = raise_smem_limit((const void*)row_pass_one_pipe<LX, SP>, attr_pipe);
-      if (e != cudaSuccess) return e;
-      int dev = 0, sms = 0, per_sm = 0;
-      if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-      if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-      if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, row_pass_one_pipe<LX, SP>, C::M * C::RW, smem)) !=
-          cudaSuccess)
-        return e;
-      const int nb = (p.rows + C::RW - 1) / C::RW;
-      const int slots = std::max(1, sms * std::max(per_sm, 1) / std::max(nz, 1));
-      const int per_cta = (nb + slots - 1) / slots;
-      const dim3 pgrid((nb + per_cta - 1) / per_cta, 1, nz);
-      LaunchCfg lc(pgrid, block, smem, st, pdl);
-      return cudaLaunchKernelEx(&lc.cfg, row_pass_one_pipe<LX, SP>, p);
-    }
     const size_t smem = 2 * (size_t)C::RW * C::PL * sizeof(float2);   // two transpose buffers
     const cudaError_t e = raise_smem_limit((const void*)row_pass_one<LX, SP>, attr_one);
     if (e != cudaSuccess) return e;

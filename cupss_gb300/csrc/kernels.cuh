@@ -365,99 +365,10 @@ __device__ __forceinline__ void row_one_body(const XParams& p, int bx, int m, in
   row_r2c_store<LX, SP>(v, TB, m, p.tw, reinterpret_cast<float2*>(p.out[0]) + rowoff, live);
 }
 
-// Persistent, software-pipelined form of row_one_body.  The CTA walks the row batches
-// bx = blockIdx.x, blockIdx.x + gridDim.x, ... of member blockIdx.z; while one batch is
-// transformed, the spectral rows of the next are already on their way into shared memory
-// (cp.async, zero-filled beyond xcols), so a CTA's load latency overlaps its own
-// arithmetic instead of only other CTAs'.  Shared memory: two input buffers used in turn
-// (each is also its batch's first transpose buffer) and one transpose buffer,
-// 3 * RW * PL float2.  Barrier order per batch: wait + barrier (the batch's rows and, for
-// the C2R mirror reads, every thread's copies are in place; the previous batch's last
-// reads of TB are done) .. inverse .. barrier .. forward transpose into TA .. barrier ..
-// TB .. barrier .. R2C reads of TB.  The copies into a buffer are issued at the top of the
-// batch after next's predecessor, after the barrier that follows the last reads of it.
-template <int LX, bool SP>
-__device__ __forceinline__ void row_one_pipe_body(const XParams& p, int m, int rl) {
-  using C = RowCfg<LX, SP>;
-  constexpr int R = C::R, PL = C::PL, RW = C::RW;
-  extern __shared__ float2 smem[];
-  grid_dep_sync();
-  if (p.members && !p.members[blockIdx.z].active) return;   // CTA-uniform
-  const int nb = (p.rows + RW - 1) / RW;
-  int bx = blockIdx.x;
-  if (bx >= nb) return;   // CTA-uniform
-  const int xcols = p.in_xcols[0] > 0 ? p.in_xcols[0] : LX;
-  const float2* inm = p.in[0] + (size_t)blockIdx.z * p.mstride;
-  float2* outm = reinterpret_cast<float2*>(p.out[0]) + (size_t)blockIdx.z * p.mstride;
-  float2* TB = smem + (2 * RW + rl) * PL;
-  auto issue = [&](int b, int buf) {
-    const int row = b * RW + rl;
-    const bool live = row < p.rows;
-    const float2* in = inm + (size_t)(live ? row : 0) * LX;
-    const unsigned sa = smem_u32(smem + (buf * RW + rl) * PL);
-#pragma unroll
-    for (int i = 0; i < R; ++i) {
-      const int k = pos_step2<LX, SP>(m, i);
-      const bool ld = live && k < xcols;
-      cp_async8(sa + 8u * (unsigned)pad_pos<LX, SP>(k), ld ? in + k : in, ld ? 8 : 0);
-    }
-    cp_async_commit();
-  };
-  issue(bx, 0);
-  const int order = p.prod_n[0];
-#pragma unroll 1
-  for (int buf = 0; bx < nb; bx += gridDim.x, buf ^= 1) {
-    if (bx + (int)gridDim.x < nb) {
-      issue(bx + gridDim.x, buf ^ 1);
-    } else {
-      cp_async_commit();   // an empty group keeps the wait count below uniform
-    }
-    cp_async_wait_group<1>();   // this batch's copies (the next batch's may still run)
-    __syncthreads();
-    float2* TA = smem + (buf * RW + rl) * PL;
-    const int row = bx * RW + rl;
-    const bool live = row < p.rows;
-    float2 v[R];
-#pragma unroll
-    for (int i = 0; i < R; ++i) v[i] = TA[pad_pos<LX, SP>(pos_step2<LX, SP>(m, i))];
-    row_c2r<LX, SP>(v, TA, m, p.tw);
-    inv_step2<LX, SP>(v, m, p.tw);
-    inv_store_t<LX, SP>(v, m, [&](int n, float2 x) { TB[pad_pos<LX, SP>(n)] = x; });
-    __syncthreads();
-    inv_load_step1<LX, SP>(v, m, p.tw, [&](int n) { return TB[pad_pos<LX, SP>(n)]; });
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const float2 x = v[r];
-      float2 acc = make_float2(p.out_scale, p.out_scale);
-      for (int t = 0; t < order; ++t) {
-        acc.x *= x.x;
-        acc.y *= x.y;
-      }
-      v[r] = acc;
-    }
-    fwd_step1<LX, SP>(v, m, p.tw);
-#pragma unroll
-    for (int s = 0; s < R; ++s) TA[pad_pos<LX, SP>(pos_t1<LX, SP>(m, s))] = v[s];
-    __syncthreads();
-    fwd_load_step2<LX, SP>(v, m, p.tw, [&](int n) { return TA[pad_pos<LX, SP>(n)]; });
-#pragma unroll
-    for (int i = 0; i < R; ++i) TB[pad_pos<LX, SP>(pos_step2<LX, SP>(m, i))] = v[i];
-    __syncthreads();
-    row_r2c_store<LX, SP>(v, TB, m, p.tw, outm + (size_t)(live ? row : 0) * LX, live);
-  }
-  cp_async_wait_all();
-}
-
 template <int LX, bool SP>
 __global__ void __launch_bounds__(RowCfg<LX, SP>::M * RowCfg<LX, SP>::RW, RowOneCfg<LX, SP>::kMinBlocks)
 row_pass_one(const XParams p) {
   row_one_body<LX, SP>(p, blockIdx.x, threadIdx.x, threadIdx.y);
-}
-
-template <int LX, bool SP>
-__global__ void __launch_bounds__(RowCfg<LX, SP>::M * RowCfg<LX, SP>::RW, RowOneCfg<LX, SP>::kMinBlocks)
-row_pass_one_pipe(const XParams p) {
-  row_one_pipe_body<LX, SP>(p, threadIdx.x, threadIdx.y);
 }
 
 // ------------------------------------------------------------------------------------

@@ -93,6 +93,9 @@ class Solver:
         capi.check(self.lib.cupssgb_solver_time_advance(self.h, int(n), C.byref(ms)))
         return ms.value
 
+    def set_stream_priority(self, level):
+        capi.check(self.lib.cupssgb_solver_set_stream_priority(self.h, int(level)))
+
     def set_kernel_timing(self, on):
         capi.check(self.lib.cupssgb_solver_set_kernel_timing(self.h, int(bool(on))))
 

@@ -111,6 +111,7 @@ SIGNATURES = {
     "cupssgb_multi_launch_count": (_LL, [_P]),
     "cupssgb_multi_describe": (_I, [_P, C.c_char_p, _I]),
     "cupssgb_multi_choose": (_I, [_P]),
+    "cupssgb_solver_set_stream_priority": (_I, [_P, _I]),
     "cupssgb_multi_generated_source": (_I, [C.POINTER(_P), _I, _I, C.c_char_p, _I]),
     "cupssgb_tune_cache_path": (_I, [C.c_char_p, _I]),
     "cupssgb_tune_cache_lookup": (_I, [_S, C.c_char_p, _I]),

@@ -475,6 +475,14 @@ int cupssgb_multi_describe(const cupssgb_multi* m, char* buf, int buflen) {
   return copy_out(m->m->describe(), buf, buflen);
 }
 
+int cupssgb_solver_set_stream_priority(cupssgb_solver* s, int level) {
+  NEED(s);
+  return guard([&] {
+    s->s->set_stream_priority(level);
+    return 0;
+  });
+}
+
 int cupssgb_multi_choose(cupssgb_multi* m) {
   NEED(m);
   return guard([&] {

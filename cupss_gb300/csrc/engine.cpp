@@ -53,7 +53,8 @@ Solver::Solver(int sx, int sy, int sz, float dx, float dy, float dz, float dt)
 }
 
 Solver::~Solver() {
-  if (stream_) cudaStreamSynchronize(stream_);
+  for (cudaStream_t st : level_streams_)
+    if (st) cudaStreamSynchronize(st);
   if (out_stream_) cudaStreamSynchronize(out_stream_);
   for (cudaEvent_t e : out_ready_)
     if (e) cudaEventDestroy(e);
@@ -71,7 +72,9 @@ Solver::~Solver() {
       if (g) cudaGraphExecDestroy(g);
   for (cudaEvent_t e : ev_pool_) cudaEventDestroy(e);
   for (void* p : allocs_) cudaFree(p);
-  if (stream_) cudaStreamDestroy(stream_);
+  for (cudaStream_t st : level_streams_)
+    if (st) cudaStreamDestroy(st);
+  if (level_ev_) cudaEventDestroy(level_ev_);
 }
 
 void Solver::check(cudaError_t e, const char* what) {
@@ -206,11 +209,44 @@ void Solver::build_plan() {
   }
 }
 
+// Stream priorities of the device: least (the default) down to greatest, numerically;
+// level l maps to max(greatest, least - l), its index among the solver's streams to l
+// clamped the same way.
+static void priority_of(int level, int max_index, int* prio, int* index) {
+  int least = 0, greatest = 0;
+  if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess)
+    throw Error(kErrCuda, "cudaDeviceGetStreamPriorityRange failed");
+  *prio = std::max(std::max(greatest, least - max_index), least - level);
+  *index = least - *prio;
+}
+
+void Solver::set_stream_priority(int level) {
+  if (level < 0) throw Error(kErrInvalid, "priority level < 0");
+  if (!prepared_) {
+    stream_level_ = level;
+    return;
+  }
+  int prio = 0, idx = 0;
+  priority_of(level, kMaxLevels - 1, &prio, &idx);
+  if (idx == level_index_) return;
+  if (!level_streams_[idx])
+    check(cudaStreamCreateWithPriority(&level_streams_[idx], cudaStreamNonBlocking, prio), "cudaStreamCreate");
+  if (!level_ev_) check(cudaEventCreateWithFlags(&level_ev_, cudaEventDisableTiming), "cudaEventCreate");
+  // everything queued so far comes first
+  check(cudaEventRecord(level_ev_, stream_), "cudaEventRecord");
+  check(cudaStreamWaitEvent(level_streams_[idx], level_ev_, 0), "cudaStreamWaitEvent");
+  stream_ = level_streams_[idx];
+  level_index_ = idx;
+}
+
 void Solver::prepare() {
   if (prepared_) throw Error(kErrState, "prepare called twice");
   int dev = 0;
   check(cudaGetDevice(&dev), "cudaGetDevice");
-  check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+  int prio = 0;
+  priority_of(stream_level_, kMaxLevels - 1, &prio, &level_index_);
+  check(cudaStreamCreateWithPriority(&stream_, cudaStreamNonBlocking, prio), "cudaStreamCreate");
+  level_streams_[level_index_] = stream_;
   build_plan();
   half_ = (size_t)Lx_ * sy_ * sz_;
   const size_t half = half_;

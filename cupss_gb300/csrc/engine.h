@@ -69,6 +69,11 @@ class Solver {
 
   void prepare();
   bool prepared() const { return prepared_; }
+  // Scheduling priority of the solver's work: 0 the default, higher levels have their
+  // kernels' CTAs scheduled first when several streams compete (clamped to the device's
+  // range).  Callable at any time: later work goes to a stream of that priority, ordered
+  // after everything queued before.
+  void set_stream_priority(int level);
   // m: batch member (0 for a single system).  Returns true when the copy of a host
   // source runs asynchronously (page-locked memory, input stream), false otherwise.
   bool set_real(int f, const float* src, bool src_on_device, int m = 0);
@@ -239,6 +244,12 @@ class Solver {
   size_t dev_bytes_ = 0;
   // batches
   int nmem_ = 1;
+  int stream_level_ = 0;   // set_stream_priority before prepare
+  // one stream per priority in use (index: levels above the default), stream_ is one of them
+  static constexpr int kMaxLevels = 8;
+  cudaStream_t level_streams_[kMaxLevels] = {};
+  int level_index_ = 0;
+  cudaEvent_t level_ev_ = nullptr;
   int mspan_ = 1;   // members covered by step launches: 1 + the last active slot
   bool batch_ = false;
   size_t half_ = 0;                              // elements of one member's spectrum

@@ -137,6 +137,13 @@ int cupssgb_solver_synchronize(cupssgb_solver* s);
  * buffers, used in turn, so that a snapshot's transform overlaps the previous snapshot's
  * copy; a snapshot waits until the copy two snapshots back has left its buffer. */
 int cupssgb_solver_snapshot_real(cupssgb_solver* s, int field, float* host_real, void* done_event);
+/* Scheduling priority of the solver's work: 0 (the default) or higher levels, whose
+ * kernels' CTAs the GPU schedules first when several streams compete (clamped to the
+ * device's priority range).  Callable at any time: work queued later runs on a stream of
+ * that priority, after everything queued before.  For a latency-critical solver sharing
+ * the GPU: a 256^2 step next to four 192^3 systems drops from about 156 to 45 us at the
+ * highest level. */
+int cupssgb_solver_set_stream_priority(cupssgb_solver* s, int level);
 /* Steps taken so far, kernels launched so far, device bytes held. */
 long long cupssgb_solver_step_count(const cupssgb_solver* s);
 long long cupssgb_solver_launch_count(const cupssgb_solver* s);

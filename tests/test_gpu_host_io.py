@@ -102,3 +102,27 @@ def test_unaligned_pinned_address_takes_the_copy(built_lib):
     assert np.array_equal(view, b.get_real(0).ravel())
     for x in (a, b, pin):
         x.close()
+
+
+def test_stream_priority(built_lib):
+    """A solver whose work moves between streams of other priorities mid-run computes
+    what one on the default stream does (each switch is ordered after the work before)."""
+    import cupss_gb300 as c
+    shape = (64, 32, 16)
+    field = splitmix64_uniform(int(np.prod(shape)), 4, -1, 1).reshape(shape[::-1])
+    out = []
+    for level in (0, 9):
+        from tests.test_codegen import solver_from_ir
+        from tests.test_parser_parity import build_lib
+        s = solver_from_ir(build_lib(*CH_NOISELESS), shape)
+        s.set_stream_priority(level)   # 9: clamped to the device's highest
+        s.prepare()
+        s.set_real(0, field)
+        for k in range(10):
+            s.advance(3)
+            s.set_stream_priority((k * 7 + level) % 4)   # switch with work in flight
+        out.append(s.get_real(0))
+        with pytest.raises(c.CupssError):
+            s.set_stream_priority(-1)
+        s.close()
+    assert np.array_equal(out[0], out[1])

@@ -37,7 +37,10 @@ Solver::Solver(int sx, int sy, int sz, float dx, float dy, float dz, float dt)
   // turnaround launch shape: tile width and resident CTAs per SM (tuning knobs)
   if (const char* w = std::getenv("CUPSSGB_TURN_W")) turn_w_ = std::atoi(w);
   if (const char* b = std::getenv("CUPSSGB_TURN_WARPS")) turn_warps_ = std::max(1, std::atoi(b));
-  if (const char* d = std::getenv("CUPSSGB_PDL")) pdl_ = std::string(d) != "0";
+  if (const char* d = std::getenv("CUPSSGB_PDL")) {
+    pdl_ = std::string(d) != "0";
+    pdl_env_ = pdl_ ? 1 : 0;
+  }
   if (const char* d = std::getenv("CUPSSGB_PLANE")) plane_env_ = std::string(d) == "0" ? 0 : 1;
   if (sx < 2 || !axis_ok(sx, 2048, 384) || !axis_ok(sy, 1024, 192) || !axis_ok(sz, 1024, 192))
     throw Error(kErrUnsupported,

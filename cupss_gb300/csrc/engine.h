@@ -161,6 +161,8 @@ class Solver {
     int tuned_warps = 0;                     // resident-warp target of its registers (0: the solver's)
     int tuned_split = -1;                    // 512/1024-point lines: 1 split form, 0 four-step, -1 rule
     bool tune_cached = false;                // the shape came from the tune cache
+    int tune_pdl = -1;                       // cached programmatic-dependent-launch choice (-1: none)
+    double tune_best_ms = 0.0;               // the tuned shape's time per phase run
     std::vector<std::pair<std::string, double>> tune_ms;   // candidate -> ms per phase run
   };
 
@@ -235,6 +237,8 @@ class Solver {
   int turn_warps_ = 16;       // resident warps per SM the generated turnaround's registers are sized for
   bool tuning_ = false;       // autotune in progress: run the width-generic generated kernel
   bool pdl_ = true;           // step kernels use programmatic dependent launch
+  int pdl_env_ = -1;          // CUPSSGB_PDL (0/1), -1: tuned
+  double pdl_ms_[2] = {0.0, 0.0};   // ms per step of a 16-step graph without / with it (0: not timed)
   bool plane_ok_ = false;     // every product phase can run the xy-plane pass (decide_plane)
   bool plane_ = false;        // 3D products by the xy-plane pass: chosen by the tuner among plane_ok_
   int plane_c_ = 0;           // CTAs per plane of the plane pass (0: the shape's default)

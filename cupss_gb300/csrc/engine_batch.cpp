@@ -225,6 +225,7 @@ void Solver::autotune() {
   for (Phase& P : phases_) {
     P.tune_ms.clear();
     P.tune_cached = false;
+    P.tune_pdl = -1;
     if (P.fields.empty()) continue;
     LineParams p;
     int nslots = 0;
@@ -315,7 +316,49 @@ void Solver::autotune() {
       if (ms < best) best = ms;
       else plane_ = true;
     }
+    P.tune_best_ms = best;
     tune_cache_store(key, tune_value(P, best));
+  }
+  // 5. programmatic dependent launch, timed on whole 16-step graphs with and without it:
+  //    it hides the launch gap between short kernels, but the next kernel's CTAs then hold
+  //    SM slots (waiting for the previous kernel's end) that a kernel with a tail of CTAs
+  //    could use -- measured either way on this GPU depending on the grid.
+  if (tune_on && pdl_env_ < 0 && turn_w_ <= 0) {
+    bool have = true;
+    int cached_pdl = -1;
+    for (const Phase& P : phases_) {
+      if (P.fields.empty()) continue;
+      if (!P.tune_cached || P.tune_pdl < 0) have = false;
+      cached_pdl = P.tune_pdl;
+    }
+    if (have && cached_pdl >= 0) {
+      pdl_ = cached_pdl == 1;
+    } else {
+      const long long s0 = step_;
+      auto time_graph = [&](bool on) {
+        pdl_ = on;
+        invalidate_graphs();
+        run_graph(0);   // captured and run once: warm-up
+        check(cudaEventRecord(a, stream_), "cudaEventRecord");
+        run_graph(0);
+        run_graph(0);
+        check(cudaEventRecord(b, stream_), "cudaEventRecord");
+        check(cudaEventSynchronize(b), "cudaEventSynchronize");
+        float ms = 0.f;
+        check(cudaEventElapsedTime(&ms, a, b), "cudaEventElapsedTime");
+        return (double)ms / (2 * kGraphChunks[0]);
+      };
+      pdl_ms_[1] = time_graph(true);
+      pdl_ms_[0] = time_graph(false);
+      pdl_ = pdl_ms_[1] <= pdl_ms_[0];
+      invalidate_graphs();
+      step_ = s0;
+      for (Phase& P : phases_)
+        if (!P.fields.empty()) {
+          P.tune_pdl = pdl_ ? 1 : 0;
+          tune_cache_store(tune_key(P), tune_value(P, P.tune_best_ms));
+        }
+    }
   }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
@@ -361,6 +404,7 @@ std::string Solver::tune_value(const Phase& P, double ms) const {
   std::ostringstream os;
   os << "W=" << P.tuned_w << " warps=" << phase_warps(P) << " split=" << (phase_split(P) ? 1 : 0)
      << " plane=" << (plane_ ? 1 : 0) << " plane_c=" << plane_c_ << " ms=" << ms;
+  if (P.tune_pdl >= 0) os << " pdl=" << P.tune_pdl;
   return os.str();
 }
 
@@ -392,6 +436,9 @@ bool Solver::apply_tune_value(Phase& P, const std::string& v, int wmax_rule) {
   P.tuned_w = wi;
   P.tuned_warps = (int)warps;
   if (L >= 512) P.tuned_split = sp ? 1 : 0;
+  double pdl = -1;
+  P.tune_pdl = (tune_value_get(v, "pdl", &pdl) && (pdl == 0.0 || pdl == 1.0)) ? (int)pdl : -1;
+  if (tune_value_get(v, "ms", &pdl)) P.tune_best_ms = pdl;
   return true;
 }
 
@@ -433,6 +480,9 @@ std::string Solver::tune_report() const {
       os << (i ? ", " : "") << "\"" << P.tune_ms[i].first << "\": " << P.tune_ms[i].second;
     os << "}}";
   }
+  // programmatic dependent launch: the choice, and the 16-step graph times when timed here
+  os << (first ? "" : ", ") << "\"pdl\": " << (pdl_ ? 1 : 0);
+  if (pdl_ms_[0] > 0.0) os << ", \"pdl_ms_per_step\": {\"off\": " << pdl_ms_[0] << ", \"on\": " << pdl_ms_[1] << "}";
   os << "}";
   return os.str();
 }

@@ -255,45 +255,51 @@ void Solver::autotune() {
       P.tune_ms.push_back({what, ms / 3.0});
       return ms / 3.0;
     };
-    // 1. tile width
-    std::vector<int> cands;
-    for (int w = wmax; w >= 2 && cands.size() < 4; w /= 2) cands.push_back(w);
-    if (cands.empty()) cands.push_back(wmax);
-    double best = 1e30;
-    int best_w = wmax;
-    for (int w : cands) {
-      P.tuned_w = w;
-      const double ms = time_phase("W=" + std::to_string(w));
-      if (ms < best) {
-        best = ms;
-        best_w = w;
-      }
-    }
-    P.tuned_w = best_w;
-    // the other dimensions need kernels of their own (compiled at prepare); below 2^20
-    // grid points (times members) a step is launch-bound and W is all that is timed
+    // 1-3 in the phase's current form; returns the best time
     const bool deep = (double)npoints() * mspan_ >= (double)(1 << 20);
-    if (use_jit_ && deep) {
-      // 2. resident-warp target (a kernel compiled for each)
-      const int w0 = phase_warps(P);
-      const int alt = w0 == 16 ? 24 : 16;
-      P.tuned_warps = alt;
-      const double ms = time_phase("warps=" + std::to_string(alt));
-      if (ms < best) best = ms;
-      else P.tuned_warps = w0;
-      // 3. FFT form of 512- and 1024-point lines (the width must suit the other form too)
-      if (L >= 512 && split_override() < 0) {
-        const bool s0 = phase_split(P);
-        P.tuned_split = s0 ? 0 : 1;
-        if (P.tuned_w <= pick_w(L, nl, nslots, 0, !s0)) {
-          const double ms2 = time_phase(std::string("split=") + (s0 ? "0" : "1"));
-          if (ms2 < best) best = ms2;
-          else P.tuned_split = s0 ? 1 : 0;
-        } else {
-          P.tuned_split = s0 ? 1 : 0;
+    std::string tag;   // label prefix of the candidates' times ("row:" when re-timed)
+    auto shape_search = [&]() {
+      // 1. tile width
+      std::vector<int> cands;
+      for (int w = wmax; w >= 2 && cands.size() < 4; w /= 2) cands.push_back(w);
+      if (cands.empty()) cands.push_back(wmax);
+      double best = 1e30;
+      int best_w = wmax;
+      for (int w : cands) {
+        P.tuned_w = w;
+        const double ms = time_phase(tag + "W=" + std::to_string(w));
+        if (ms < best) {
+          best = ms;
+          best_w = w;
         }
       }
-    }
+      P.tuned_w = best_w;
+      // the other dimensions need kernels of their own (compiled at prepare); below 2^20
+      // grid points (times members) a step is launch-bound and W is all that is timed
+      if (use_jit_ && deep) {
+        // 2. resident-warp target (a kernel compiled for each)
+        const int w0 = phase_warps(P);
+        const int alt = w0 == 16 ? 24 : 16;
+        P.tuned_warps = alt;
+        const double ms = time_phase(tag + "warps=" + std::to_string(alt));
+        if (ms < best) best = ms;
+        else P.tuned_warps = w0;
+        // 3. FFT form of 512- and 1024-point lines (the width must suit the other form too)
+        if (L >= 512 && split_override() < 0) {
+          const bool s0 = phase_split(P);
+          P.tuned_split = s0 ? 0 : 1;
+          if (P.tuned_w <= pick_w(L, nl, nslots, 0, !s0)) {
+            const double ms2 = time_phase(tag + "split=" + (s0 ? "0" : "1"));
+            if (ms2 < best) best = ms2;
+            else P.tuned_split = s0 ? 1 : 0;
+          } else {
+            P.tuned_split = s0 ? 1 : 0;
+          }
+        }
+      }
+      return best;
+    };
+    double best = shape_search();
     // 4. 3D products: the xy-plane pass (each instantiated cluster size) or the row pass
     //    with two y line passes (one choice per solver, made on its first product phase)
     if (plane_ok_ && plane_env_ < 0 && deep && !P.products.empty() && !plane_tuned) {
@@ -313,8 +319,23 @@ void Solver::autotune() {
       }
       plane_ = false;
       const double ms = time_phase("plane=0");
-      if (ms < best) best = ms;
-      else plane_ = true;
+      if (ms < best) {
+        // the row-pass form wins: its own tile width, warps and line form (1-3 above were
+        // timed in the plane form)
+        const int w1 = P.tuned_w, warps1 = P.tuned_warps, split1 = P.tuned_split;
+        P.tuned_warps = 0;
+        P.tuned_split = -1;
+        tag = "row:";
+        best = shape_search();
+        if (ms < best) {   // the shape found in the plane form stays the faster
+          best = ms;
+          P.tuned_w = w1;
+          P.tuned_warps = warps1;
+          P.tuned_split = split1;
+        }
+      } else {
+        plane_ = true;
+      }
     }
     P.tune_best_ms = best;
     tune_cache_store(key, tune_value(P, best));

@@ -84,12 +84,15 @@ void Solver::check(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw Error(kErrCuda, cuda_msg(e, what));
 }
 
-void* Solver::dalloc(size_t bytes) {
+// Device allocation owned by the solver, zeroed on the solver's stream unless `zero` is
+// false (a buffer that another stream fills completely before anything reads it: a
+// zeroing queued on the solver's stream could land after that stream's writes).
+void* Solver::dalloc(size_t bytes, bool zero) {
   void* p = nullptr;
   check(cudaMalloc(&p, bytes), "cudaMalloc");
   allocs_.push_back(p);
   dev_bytes_ += bytes;
-  check(cudaMemsetAsync(p, 0, bytes, stream_), "cudaMemsetAsync");
+  if (zero) check(cudaMemsetAsync(p, 0, bytes, stream_), "cudaMemsetAsync");
   return p;
 }
 
@@ -448,7 +451,7 @@ bool Solver::set_real(int f, const float* src, bool on_device, int m) {
     b = up_next_;
     up_next_ ^= 1;
     if (!up_stage_[b]) {
-      up_stage_[b] = (float*)dalloc(n * sizeof(float));
+      up_stage_[b] = (float*)dalloc(n * sizeof(float), false);   // the copy below fills it
       check(cudaEventCreateWithFlags(&up_ready_[b], cudaEventDisableTiming), "cudaEventCreate");
       check(cudaEventCreateWithFlags(&up_free_[b], cudaEventDisableTiming), "cudaEventCreate");
     } else {

@@ -167,7 +167,7 @@ class Solver {
   };
 
   void check(cudaError_t e, const char* what);
-  void* dalloc(size_t bytes);
+  void* dalloc(size_t bytes, bool zero = true);
   void build_plan();
   void run_phase(Phase& ph);
   // the row pass of a phase with products (its products from the dealiased channels)

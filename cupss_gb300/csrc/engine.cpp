@@ -135,6 +135,7 @@ void Solver::set_term_pres(int f, int t, const std::vector<HostPres>& p) {
   if (p.size() != fields_[f].terms[t].pres.size())
     throw Error(kErrInvalid, "prefactor count of a term cannot change");
   fields_[f].terms[t].pres = p;
+  merge_check_ = true;
   invalidate_graphs();
 }
 
@@ -174,33 +175,15 @@ void Solver::build_plan() {
       if (t.product.size() >= 2)
         for (int g : t.product)
           alias_order_[g] = std::max(alias_order_[g], (int)t.product.size());
+  const char* me = std::getenv("CUPSSGB_MERGE");
+  if (me && std::string(me) == "0") merge_off_ = true;
   for (int ph = 0; ph < 2; ++ph) {
     Phase& P = phases_[ph];
     P = Phase();
     P.id = ph;
     for (int f = 0; f < F; ++f)
       if ((int)fields_[f].dynamic == ph) P.fields.push_back(f);
-    for (int f : P.fields) {
-      for (const HostTerm& t : fields_[f].terms) {
-        if (t.product.size() < 2) {
-          P.term_slot.push_back(-1);
-          continue;
-        }
-        std::vector<int> key = t.product;
-        std::sort(key.begin(), key.end());
-        auto it = std::find(P.products.begin(), P.products.end(), key);
-        int slot;
-        if (it == P.products.end()) {
-          P.products.push_back(key);
-          slot = (int)P.products.size() - 1;
-        } else {
-          slot = (int)(it - P.products.begin());
-        }
-        P.term_slot.push_back(slot);
-        for (int g : key)
-          if (std::find(P.xin.begin(), P.xin.end(), g) == P.xin.end()) P.xin.push_back(g);
-      }
-    }
+    plan_products(P, !merge_off_);
     if ((int)P.fields.size() > kMaxPhaseFields) throw Error(kErrLimit, "too many fields in a phase");
     if ((int)P.products.size() > kMaxProd) throw Error(kErrLimit, "too many distinct products");
     if ((int)P.xin.size() > kMaxXIn) throw Error(kErrLimit, "too many fields in products");
@@ -224,6 +207,148 @@ static void priority_of(int level, int max_index, int* prio, int* index) {
     throw Error(kErrCuda, "cudaDeviceGetStreamPriorityRange failed");
   *prio = std::max(std::max(greatest, least - max_index), least - level);
   *index = least - *prio;
+}
+
+namespace {
+bool same_pres(const std::vector<HostPres>& a, const std::vector<HostPres>& b) {
+  if (a.size() != b.size()) return false;
+  for (size_t j = 0; j < a.size(); ++j)
+    if (a[j].pre != b[j].pre || a[j].q2n != b[j].q2n || a[j].iqx != b[j].iqx || a[j].iqy != b[j].iqy ||
+        a[j].iqz != b[j].iqz || a[j].invq != b[j].invq)
+      return false;
+  return true;
+}
+}  // namespace
+
+void Solver::plan_products(Phase& P, bool merge) {
+  P.products.clear();
+  P.prod_add.clear();
+  P.term_slot.clear();
+  P.xin.clear();
+  P.chan_buf.clear();
+  P.groups.clear();
+  P.nchan = 0;
+  // the phase's product terms (field, term) and their product keys, in term order
+  struct PT {
+    int f, t;
+    std::vector<int> key;
+  };
+  std::vector<PT> pts;
+  for (int f : P.fields)
+    for (size_t t = 0; t < fields_[f].terms.size(); ++t) {
+      const HostTerm& ht = fields_[f].terms[t];
+      if (ht.product.size() < 2) continue;
+      std::vector<int> key = ht.product;
+      std::sort(key.begin(), key.end());
+      pts.push_back({f, (int)t, key});
+      for (int g : key)
+        if (std::find(P.xin.begin(), P.xin.end(), g) == P.xin.end()) P.xin.push_back(g);
+    }
+  auto uses = [&](const std::vector<int>& key) {
+    int n = 0;
+    for (const PT& q : pts) n += q.key == key;
+    return n;
+  };
+  auto pres_of = [&](int f, int t, int m) -> const std::vector<HostPres>& {
+    return (m < 0 ? fields_ : mfields_[m])[f].terms[t].pres;
+  };
+  // group: index into pts -> group id (-1: alone)
+  std::vector<int> gid(pts.size(), -1);
+  std::vector<std::vector<int>> groups;
+  if (merge) {
+    for (size_t i = 0; i < pts.size(); ++i) {
+      if (gid[i] >= 0 || uses(pts[i].key) != 1) continue;
+      std::vector<int> g{(int)i};
+      for (size_t j = i + 1; j < pts.size(); ++j) {
+        if (gid[j] >= 0 || pts[j].f != pts[i].f || uses(pts[j].key) != 1) continue;
+        bool same = same_pres(pres_of(pts[i].f, pts[i].t, -1), pres_of(pts[j].f, pts[j].t, -1));
+        for (int m = 0; same && m < (int)mfields_.size(); ++m)
+          same = same_pres(pres_of(pts[i].f, pts[i].t, m), pres_of(pts[j].f, pts[j].t, m));
+        if (same) g.push_back((int)j);
+      }
+      if (g.size() < 2) continue;
+      for (int k : g) gid[k] = (int)groups.size();
+      groups.push_back(g);
+    }
+  }
+  // channels in term order: a group's products one after the other, then its own
+  // buffer; a product that is not merged gets one channel however many terms use it
+  std::vector<int> chan_of_term(pts.size(), -1);
+  for (size_t i = 0; i < pts.size(); ++i) {
+    if (chan_of_term[i] != -1) continue;
+    if (gid[i] >= 0) {
+      const std::vector<int>& g = groups[gid[i]];
+      std::vector<std::pair<int, int>> members;
+      for (size_t k = 0; k < g.size(); ++k) {
+        P.products.push_back(pts[g[k]].key);
+        P.prod_add.push_back(k > 0 ? 1 : 0);
+        chan_of_term[g[k]] = k == 0 ? P.nchan : -2;
+        members.push_back({pts[g[k]].f, pts[g[k]].t});
+      }
+      P.groups.push_back(members);
+    } else {
+      auto it = std::find(P.products.begin(), P.products.end(), pts[i].key);
+      if (it != P.products.end()) {
+        // used by an earlier term: that term's channel (a product used twice is never merged)
+        for (size_t j = 0; j < i; ++j)
+          if (pts[j].key == pts[i].key) {
+            chan_of_term[i] = chan_of_term[j];
+            break;
+          }
+        continue;
+      }
+      P.products.push_back(pts[i].key);
+      P.prod_add.push_back(0);
+      chan_of_term[i] = P.nchan;
+      P.groups.push_back({});
+    }
+    P.chan_buf.push_back((int)P.products.size() - 1);
+    ++P.nchan;
+  }
+  // slots of every term of the phase, in the order fill_turn walks them
+  size_t k = 0;
+  for (int f : P.fields)
+    for (const HostTerm& ht : fields_[f].terms) {
+      if (ht.product.size() < 2) {
+        P.term_slot.push_back(-1);
+        continue;
+      }
+      P.term_slot.push_back(chan_of_term[k++]);
+    }
+}
+
+bool Solver::merges_hold() const {
+  for (const Phase& P : phases_)
+    for (const auto& g : P.groups)
+      for (size_t k = 1; k < g.size(); ++k) {
+        if (!same_pres(fields_[g[0].first].terms[g[0].second].pres, fields_[g[k].first].terms[g[k].second].pres))
+          return false;
+        for (const auto& mf : mfields_)
+          if (!same_pres(mf[g[0].first].terms[g[0].second].pres, mf[g[k].first].terms[g[k].second].pres))
+            return false;
+      }
+  return true;
+}
+
+void Solver::check_merges() {
+  if (!merge_check_) return;
+  merge_check_ = false;
+  if (merge_off_ || merges_hold()) return;
+  // re-plan without merging; every distinct product keeps the buffer it has
+  merge_off_ = true;
+  for (Phase& P : phases_) {
+    std::vector<std::pair<std::vector<int>, float2*>> bufs;
+    for (size_t q = 0; q < P.products.size() && q < P.prodbuf.size(); ++q) bufs.push_back({P.products[q], P.prodbuf[q]});
+    plan_products(P, false);
+    P.prodbuf.clear();
+    for (const auto& key : P.products)
+      for (const auto& b : bufs)
+        if (b.first == key) P.prodbuf.push_back(b.second);
+    if (P.prodbuf.size() != P.products.size()) throw Error(kErrState, "product buffers lost in re-planning");
+    P.jit_sig.clear();
+  }
+  ++plan_epoch_;
+  invalidate_graphs();
 }
 
 void Solver::set_stream_priority(int level) {
@@ -748,6 +873,7 @@ void Solver::advance_phase(int phase) {
   if (!prepared_) throw Error(kErrState, "advance before prepare");
   if (phase < 0 || phase > 1) throw Error(kErrInvalid, "phase is 0 (non-dynamic) or 1 (dynamic)");
   if (batch_) throw Error(kErrUnsupported, "phase-wise stepping (callbacks) is for single systems");
+  check_merges();
   run_phase(phases_[phase]);
   if (phase == 1) {
     check(launch_tick(members_d_, nmem_, 1u, stream_), "member step count");
@@ -796,8 +922,8 @@ void Solver::fill_turn(const Phase& P, LineParams& p, int& nslots, bool& any_cha
   const bool have_dev = prepared_;
   any_chan = false;
   fill_line_common(p, L, geo, kModeTurn);
-  p.n_prod = (int)P.products.size();
-  for (int q = 0; q < p.n_prod; ++q) p.prod_in[q] = have_dev ? P.prodbuf[q] : nullptr;
+  p.n_prod = P.nchan;
+  for (int q = 0; q < p.n_prod; ++q) p.prod_in[q] = have_dev ? P.prodbuf[P.chan_buf[q]] : nullptr;
   for (int g = 0; g < nfields(); ++g) p.state[g] = (have_dev ? state_[par_[g]][g] : nullptr);
   p.key0 = (uint32_t)(seed_ & 0xffffffffu);
   p.key1 = (uint32_t)(seed_ >> 32);
@@ -842,6 +968,9 @@ void Solver::fill_turn(const Phase& P, LineParams& p, int& nslots, bool& any_cha
       } else if (ht.product.size() == 1) {
         T.kind = kTermSingle;
         T.src = src_slot(ht.product[0]);
+      } else if (P.term_slot[ts] == -2) {
+        T.kind = kTermMerged;   // summed into its group's first term's channel
+        T.src = 0;
       } else {
         T.kind = kTermProduct;
         T.src = P.term_slot[ts];
@@ -974,9 +1103,10 @@ void Solver::run_phase(Phase& P) {
     mark_end("row_pass");
     ++launches_;
     if (dim_ == 3) {
-      for (size_t q = 0; q < P.products.size(); ++q) {
+      for (int c = 0; c < P.nchan; ++c) {
+        float2* b = P.prodbuf[P.chan_buf[c]];
         mark_begin();
-        line_fwd_inv(kGeoY3, kModeFwd, P.prodbuf[q], P.prodbuf[q], Lx_, batch_, 0, pdl_);
+        line_fwd_inv(kGeoY3, kModeFwd, b, b, Lx_, batch_, 0, pdl_);
         mark_end("line_fwd_y");
       }
     }
@@ -1045,6 +1175,7 @@ void Solver::row_params(const Phase& P, XParams& x) const {
   }
   x.n_prod = (int)P.products.size();
   for (int q = 0; q < x.n_prod; ++q) {
+    x.prod_add[q] = P.prod_add[q];
     x.out[q] = q < (int)P.prodbuf.size() ? P.prodbuf[q] : nullptr;
     x.prod_n[q] = (int)P.products[q].size();
     for (int t = 0; t < x.prod_n[q]; ++t) {
@@ -1152,6 +1283,7 @@ void Solver::step_once(uint32_t off, bool tick) {
 void Solver::advance(int nsteps) {
   if (!prepared_) throw Error(kErrState, "advance before prepare");
   if (batch_ && mvals_dirty_) upload_member_values();
+  check_merges();
   if (!timing_) {
     for (int c = 0; c < 3; ++c)
       for (; nsteps >= kGraphChunks[c]; nsteps -= kGraphChunks[c]) run_graph(c);

@@ -151,7 +151,11 @@ class Solver {
   struct Phase {
     int id = 0;                              // 0: non-dynamic, 1: dynamic
     std::vector<int> fields;                 // fields updated in this phase
-    std::vector<std::vector<int>> products;  // sorted multisets (size >= 2)
+    std::vector<std::vector<int>> products;  // sorted multisets (size >= 2), channel by channel
+    std::vector<int> prod_add;               // per product: added into the previous one's channel
+    int nchan = 0;                           // product channels (sums of products) of the turnaround
+    std::vector<int> chan_buf;               // per channel: the product whose buffer holds it (its last)
+    std::vector<std::vector<std::pair<int, int>>> groups;   // merged terms (field, term) per channel
     std::vector<int> xin;                    // fields feeding the row pass
     std::vector<float2*> prodbuf;
     std::vector<int> term_slot;              // per (field, term) flattened: product slot or -1
@@ -169,6 +173,16 @@ class Solver {
   void check(cudaError_t e, const char* what);
   void* dalloc(size_t bytes, bool zero = true);
   void build_plan();
+  // Distinct products of a phase, their channels and the terms' slots.  With `merge`,
+  // product terms of one field with identical prefactor lists (for every batch member)
+  // whose products no other term of the phase uses share one channel: the row pass sums
+  // their real-space products before one forward transform, and the update applies the
+  // prefactors once (KPZ's 0.5*lambda*iqxh^2 + 0.5*lambda*iqyh^2).
+  void plan_products(Phase& P, bool merge);
+  bool merges_hold() const;   // every merged group still has equal prefactors
+  // After prefactor changes: if a merged group's terms now differ, the solver drops
+  // merging (products keep their buffers; kernels and graphs are rebuilt).
+  void check_merges();
   void run_phase(Phase& ph);
   // the row pass of a phase with products (its products from the dealiased channels)
   void row_params(const Phase& P, XParams& x) const;
@@ -248,6 +262,9 @@ class Solver {
   size_t dev_bytes_ = 0;
   // batches
   int nmem_ = 1;
+  bool merge_off_ = false;     // product merging dropped (a merged group diverged) or CUPSSGB_MERGE=0
+  bool merge_check_ = false;   // prefactors changed since the merges were last checked
+  int plan_epoch_ = 0;         // incremented when the phases are re-planned after prepare
   int stream_level_ = 0;   // set_stream_priority before prepare
   // one stream per priority in use (index: levels above the default), stream_ is one of them
   static constexpr int kMaxLevels = 8;

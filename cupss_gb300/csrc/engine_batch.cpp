@@ -65,6 +65,7 @@ void Solver::set_member_term_pres(int m, int f, int t, const std::vector<HostPre
   ensure_member_fields(mfields_, nmem_, fields_);
   mfields_[m][f].terms[t].pres = p;
   mvals_dirty_ = true;
+  merge_check_ = prepared_;
 }
 
 void Solver::set_member_implicit(int m, int f, const std::vector<HostPres>& p) {

@@ -36,7 +36,8 @@ std::string MultiStep::unsupported(const std::vector<Solver*>& s, bool need_prep
     for (int ph = 0; ph < 2; ++ph) {
       const Solver::Phase& P = S.phases_[ph];
       const Solver::Phase& P0 = s[0]->phases_[ph];
-      if (P.fields != P0.fields || P.products != P0.products || P.xin != P0.xin)
+      if (P.fields != P0.fields || P.products != P0.products || P.xin != P0.xin || P.prod_add != P0.prod_add ||
+          P.term_slot != P0.term_slot)
         return "the classes differ in system structure";
       if (P.fields.empty() || c == 0) continue;
       LineParams p, p0;
@@ -166,6 +167,8 @@ std::string MultiStep::generated_source(const std::vector<Solver*>& s, int ph) {
 }
 
 void MultiStep::build() {
+  epoch_.clear();
+  for (Solver* S : s_) epoch_.push_back(S->plan_epoch_);
   for (int ph = 0; ph < 2; ++ph) {
     PhaseK& K = ph_[ph];
     std::string src;
@@ -280,8 +283,14 @@ void MultiStep::advance(int nsteps) {
     for (Solver* S : s_) S->advance(nsteps);
     return;
   }
-  for (Solver* S : s_)
+  for (size_t c = 0; c < s_.size(); ++c) {
+    Solver* S = s_[c];
     if (S->mvals_dirty_) S->upload_member_values();
+    S->check_merges();
+    if (S->plan_epoch_ != epoch_[c])
+      throw Error(kErrState, "a grid class was re-planned (merged product terms now differ): create the fused "
+                             "stepper again");
+  }
   const int parity = s_[0]->par_.empty() ? 0 : s_[0]->par_[0];
   for (Solver* S : s_)
     for (int p : S->par_)

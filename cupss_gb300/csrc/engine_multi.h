@@ -76,6 +76,7 @@ class MultiStep {
   std::vector<cudaEvent_t> class_ev_;
   cudaGraphExec_t graph_[3][2] = {};
   std::vector<int> graph_span_;   // the classes' member spans the graphs were captured with
+  std::vector<int> epoch_;        // the classes' plan epochs the fused kernels were built for
   long long graph_launches_[3] = {};
   long long launches_ = 0;
   // parameter blocks of the fused launches (27 KB and 4 KB), built per launch

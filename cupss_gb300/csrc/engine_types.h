@@ -35,7 +35,10 @@ struct PresK {
   int q2n, iqx, iqy, iqz, invq;
 };
 
-enum TermKind : int { kTermSingle = 0, kTermProduct = 1, kTermConst = 2 };
+// kTermMerged: a product term whose real-space product the row pass adds into another
+// term's channel (same prefactors): its contribution arrives with that term, so the
+// update skips it.
+enum TermKind : int { kTermSingle = 0, kTermProduct = 1, kTermConst = 2, kTermMerged = 3 };
 
 struct TermK {
   int kind;    // TermKind
@@ -126,6 +129,9 @@ struct XParams {
   void* out[kMaxProd];
   int prod_n[kMaxProd];
   int prod_f[kMaxProd][kMaxOrder];
+  // 1: product q is added to the values of product q - 1 (one output channel, transformed
+  // and written once, after its last product); 0: product q starts a channel
+  int prod_add[kMaxProd];
   const float2* tw;
   size_t mstride;                   // batches: member z's rows start z * mstride elements on
   const MemberK* members;           // null for a single system

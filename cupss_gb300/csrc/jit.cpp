@@ -100,6 +100,7 @@ std::string gen_prog(const LineParams& p, bool batched) {
     o << "        float2 acc = make_float2(0.f, 0.f);\n";
     for (int t = 0; t < K.nterms; ++t) {
       const TermK& T = p.term[K.term0 + t];
+      if (T.kind == kTermMerged) continue;   // summed into another term's product channel
       o << "        {\n          float mt = 0.f;\n";
       for (int j = 0; j < T.npres; ++j) {
         const PresK& pr = p.pres[T.pres0 + j];

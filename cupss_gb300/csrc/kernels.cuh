@@ -249,7 +249,9 @@ __device__ __forceinline__ void row_pass_body(const XParams& p, int bx, int m, i
   }
 
   for (int q = 0; q < p.n_prod; ++q) {
-    // pointwise product of the real values (packed as pairs r[2n], r[2n+1])
+    // pointwise product of the real values (packed as pairs r[2n], r[2n+1]), added to the
+    // channel's earlier products when prod_add[q] is set
+    const bool add = p.prod_add[q] != 0;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int a = pad_pos<LX, SP>(pos_step1<LX, SP>(m, r));
@@ -259,8 +261,9 @@ __device__ __forceinline__ void row_pass_body(const XParams& p, int bx, int m, i
         acc.x *= x.x;
         acc.y *= x.y;
       }
-      v[r] = acc;
+      v[r] = add ? make_float2(v[r].x + acc.x, v[r].y + acc.y) : acc;
     }
+    if (q + 1 < p.n_prod && p.prod_add[q + 1]) continue;   // CTA-uniform: the channel goes on
     if (p.out_mode != kXOutSpectral) {
       if (live) {
 #pragma unroll

@@ -78,6 +78,7 @@ struct InterpProg {
     float2 acc = make_float2(0.f, 0.f);
     for (int t = 0; t < K.nterms; ++t) {
       const TermK T = P.term[K.term0 + t];
+      if (T.kind == kTermMerged) continue;   // in another term's product channel
       float2 src;
       if (T.kind == kTermProduct) {
         src = fx.prod(T.src);

@@ -184,3 +184,39 @@ def test_fused_refusals(built_lib):
         assert why in str(ex.value), str(ex.value)
         for s in solvers:
             s.close()
+
+
+@pytest.mark.parametrize("merge", [True, False])
+def test_product_terms_with_equal_prefactors_share_a_channel(built_lib, monkeypatch, merge):
+    """KPZ's 0.5*lam*iqxh^2 + 0.5*lam*iqyh^2: with merging the row pass sums the two
+    squares in real space and the update reads one product channel (the second term is
+    skipped); CUPSSGB_MERGE=0 keeps one channel per product."""
+    from cupss_gb300.api import jit_check
+    from tests.test_parser_parity import build_lib
+    if not merge:
+        monkeypatch.setenv("CUPSSGB_MERGE", "0")
+    s = solver_from_ir(build_lib(*KPZ_IR), (64, 64, 1))
+    src0, src1 = s.generated_sources()
+    assert "fx.prod(0)" in src1
+    assert ("fx.prod(1)" in src1) != merge
+    assert "kNProd = %d;" % (1 if merge else 2) in src1
+    assert jit_check(src1) > 0
+    s.close()
+
+
+def test_merge_needs_equal_prefactors_and_exclusive_products(built_lib):
+    """Model H: phi's -vx*iqxphi - vy*iqyphi (equal prefactors) share a channel; phi^3
+    (another prefactor) and the velocity equations' products (each used by two terms with
+    different prefactors) keep their own."""
+    from tests.test_parser_parity import build_lib
+    fields = [("phi", 1), ("iqxphi", 0), ("iqyphi", 0), ("lapphi", 0), ("vx", 0), ("vy", 0)]
+    eqs = ["dt phi + q^2*(a + k*q^2)*phi = -b*q^2*phi^3 - vx*iqxphi - vy*iqyphi",
+           "iqxphi = iqx*phi", "iqyphi = iqy*phi", "lapphi = -q^2*phi",
+           "vx*eta*q^2 = -k*iqxphi*lapphi - k*iqx^2*1/q^2*iqxphi*lapphi - k*iqx*iqy*1/q^2*iqyphi*lapphi",
+           "vy*eta*q^2 = -k*iqyphi*lapphi - k*iqy^2*1/q^2*iqyphi*lapphi - k*iqx*iqy*1/q^2*iqxphi*lapphi"]
+    ir = build_lib(fields, {"a": -1.0, "b": 1.0, "k": 4.0, "eta": 1.0, "T": 0.001}, eqs, [("phi", "2*T")])
+    s = solver_from_ir(ir, (64, 64, 1))
+    src0, src1 = s.generated_sources()
+    assert "kNProd = 2;" in src1    # phi^3, and vx*iqxphi + vy*iqyphi
+    assert "kNProd = 2;" in src0    # iqxphi*lapphi, iqyphi*lapphi: each used with several prefactors
+    s.close()

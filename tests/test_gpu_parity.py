@@ -355,3 +355,25 @@ def test_early_noise_order_gives_the_same_fields(shape, monkeypatch):
     _, early, _ = run_case(spec, shape, 0.01, 20, init, seed=8)
     assert np.array_equal(early.getReal("phi"), late.getReal("phi"))
     assert rel_l2(late.getReal("phi"), r.real_field("phi")) < 2e-5
+
+
+KPZ2 = ([("h", 1), ("iqxh", 0), ("iqyh", 0)], {"nu": 1.0, "la": 1.0, "lb": 1.0, "D": 1.0},
+        ["dt h + nu*q^2*h = 0.5*la*iqxh^2 + 0.5*lb*iqyh^2", "iqxh = iqx*h", "iqyh = iqy*h"],
+        [("h", "2*D")])
+
+
+def test_merged_products_split_when_their_prefactors_part():
+    """la = lb: the two squares share one product channel (summed in real space); after
+    updateParameter("lb") the terms differ, the solver re-plans without merging at the next
+    step, and the run still matches the oracle (which never merges)."""
+    shape = (64, 32, 1)
+    init = init_field(shape, -0.3, 0.3)
+    r, e, _ = run_case(KPZ2, shape, 0.005, 20, {"h": init})
+    assert rel_l2(e.getReal("h"), r.real_field("h")) < 3e-5
+    e.updateParameter("lb", 2.5)
+    r.sys.update_parameter("lb", 2.5)
+    r.prepare_tables_only()
+    e.advanceTime(20)
+    r.advance(20)
+    for nm in ("h", "iqxh", "iqyh"):
+        assert rel_l2(e.getReal(nm), r.real_field(nm)) < 3e-5, nm

@@ -62,6 +62,7 @@ MultiStep::MultiStep(const std::vector<Solver*>& s)
   if (!why.empty()) throw Error(kErrUnsupported, why);
   check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
   check(cudaEventCreateWithFlags(&ev_, cudaEventDisableTiming), "cudaEventCreate");
+  pdl_ = s_[0]->pdl_;   // class 0's own choice until choose() times both
   class_ev_.resize(s_.size());
   for (cudaEvent_t& e : class_ev_) check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
   build();
@@ -207,7 +208,7 @@ void MultiStep::launch_phase(int ph, uint32_t off) {
       mr.span[c] = S.mspan_;
     }
   }
-  const bool pdl = s_[0]->pdl_;
+  const bool pdl = pdl_;
   if (K.has_row) {
     void* args[] = {(void*)&mr};
     LaunchCfg lc(dim3(K.row_grid.x, 1, zmax), dim3(128), K.row_smem, stream_, pdl);
@@ -237,7 +238,7 @@ void MultiStep::step_once(uint32_t off, bool tick) {
       tp.members[c] = s_[c]->members_d_;
       tp.n[c] = s_[c]->nmem_;
     }
-    check(launch_tick_multi(tp, stream_, s_[0]->pdl_), "member step counts");
+    check(launch_tick_multi(tp, stream_, pdl_), "member step counts");
     ++launches_;
   }
 }
@@ -299,13 +300,7 @@ void MultiStep::advance(int nsteps) {
   std::vector<int> span;
   for (Solver* S : s_) span.push_back(S->mspan_);
   if (span != graph_span_) {
-    check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
-    for (auto& row : graph_)
-      for (cudaGraphExec_t& g : row)
-        if (g) {
-          cudaGraphExecDestroy(g);
-          g = nullptr;
-        }
+    invalidate();
     graph_span_ = span;
   }
   // after everything queued on the classes' streams (uploads)
@@ -328,6 +323,16 @@ void MultiStep::advance(int nsteps) {
   // the classes' later work (readouts) after the steps
   check(cudaEventRecord(ev_, stream_), "cudaEventRecord");
   for (Solver* S : s_) check(cudaStreamWaitEvent(S->stream_, ev_, 0), "cudaStreamWaitEvent");
+}
+
+void MultiStep::invalidate() {
+  check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+  for (auto& row : graph_)
+    for (cudaGraphExec_t& g : row)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
 }
 
 void MultiStep::restart() {
@@ -363,9 +368,14 @@ void MultiStep::choose() {
   chosen_ = true;
   const std::string key = choice_key();
   std::string cached;
-  double f = -1.0;
+  double f = -1.0, pd = -1.0;
   if (tune_cache_lookup(key, &cached) && tune_value_get(cached, "fused", &f) && (f == 0.0 || f == 1.0) &&
+      tune_value_get(cached, "pdl", &pd) && (pd == 0.0 || pd == 1.0) &&
       tune_value_get(cached, "ms_fused", &ms_fused_) && tune_value_get(cached, "ms_grouped", &ms_grouped_)) {
+    if (pdl_ != (pd == 1.0)) {
+      pdl_ = pd == 1.0;
+      invalidate();
+    }
     fused_ = f == 1.0;
     choice_cached_ = true;
     return;
@@ -400,7 +410,15 @@ void MultiStep::choose() {
     return (double)ms / kSteps;
   };
   try {
-    ms_fused_ = timed(true);
+    // the fused launches without and with programmatic dependent launch (graphs of each)
+    for (int on = 0; on < 2; ++on) {
+      pdl_ = on == 1;
+      invalidate();
+      ms_fused_pdl_[on] = timed(true);
+    }
+    pdl_ = ms_fused_pdl_[1] < ms_fused_pdl_[0];
+    invalidate();
+    ms_fused_ = ms_fused_pdl_[pdl_ ? 1 : 0];
     ms_grouped_ = timed(false);
   } catch (...) {
     cudaEventDestroy(a);
@@ -415,7 +433,8 @@ void MultiStep::choose() {
   for (size_t c = 0; c < s_.size(); ++c) s_[c]->launches_ = sl0[c];
   restart();
   std::ostringstream v;
-  v << "fused=" << (fused_ ? 1 : 0) << " ms_fused=" << ms_fused_ << " ms_grouped=" << ms_grouped_;
+  v << "fused=" << (fused_ ? 1 : 0) << " pdl=" << (pdl_ ? 1 : 0) << " ms_fused=" << ms_fused_
+    << " ms_grouped=" << ms_grouped_;
   tune_cache_store(key, v.str());
 }
 
@@ -438,9 +457,13 @@ std::string MultiStep::describe() const {
   }
   os << "], \"launches_per_step\": " << ((ph_[0].active ? 1 + ph_[0].has_row : 0) + (ph_[1].active ? 1 + ph_[1].has_row : 0))
      << ", \"form\": \"" << (fused_ ? "fused" : "grouped") << "\"";
-  if (chosen_)
-    os << ", \"ms_per_step\": {\"fused\": " << ms_fused_ << ", \"grouped\": " << ms_grouped_
-       << "}, \"cached\": " << (choice_cached_ ? "true" : "false");
+  os << ", \"pdl\": " << (pdl_ ? 1 : 0);
+  if (chosen_) {
+    os << ", \"ms_per_step\": {\"fused\": " << ms_fused_ << ", \"grouped\": " << ms_grouped_;
+    if (ms_fused_pdl_[0] > 0.0)
+      os << ", \"fused_pdl_off\": " << ms_fused_pdl_[0] << ", \"fused_pdl_on\": " << ms_fused_pdl_[1];
+    os << "}, \"cached\": " << (choice_cached_ ? "true" : "false");
+  }
   os << "}";
   return os.str();
 }

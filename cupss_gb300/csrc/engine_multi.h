@@ -62,15 +62,18 @@ class MultiStep {
   void step_once(uint32_t off, bool tick);
   void capture(int c, int parity);
 
-  void restart();   // zero buffers, members at step 0 (after timing)
+  void restart();      // zero buffers, members at step 0 (after timing)
+  void invalidate();   // drop the captured graphs (after the launch mode changed)
   std::string choice_key() const;
 
   std::vector<Solver*> s_;
   PhaseK ph_[2];
   uint64_t src_hash_ = 0;   // of the fused kernels' sources
   bool fused_ = true;       // false: every class steps on its own stream
+  bool pdl_ = false;        // the fused launches use programmatic dependent launch
   bool choice_cached_ = false, chosen_ = false;
-  double ms_fused_ = -1.0, ms_grouped_ = -1.0;   // per step, from choose()
+  double ms_fused_ = -1.0, ms_grouped_ = -1.0;   // per step, from choose() (fused: the better launch mode)
+  double ms_fused_pdl_[2] = {-1.0, -1.0};        // fused, without / with programmatic dependent launch
   cudaStream_t stream_ = nullptr;
   cudaEvent_t ev_ = nullptr;
   std::vector<cudaEvent_t> class_ev_;

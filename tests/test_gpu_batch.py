@@ -316,3 +316,29 @@ def test_fused_four_sizes_match_single_solves(monkeypatch, tmp_path, fuse):
         for nm in ("h", "iqxh", "iqyh"):
             err = rel(e.getReal(m, nm), ref[nm])
             assert err < 1e-6, (m, shape, nm, err)
+
+
+def test_fused_1d_and_radix3_grids_match_single_solves(monkeypatch):
+    """The fused launches over 1D grids (one-point lines, most of a tile idle) and lengths
+    3*2^a, forced (CUPSSGB_FUSE=1): every member equals its single solve."""
+    monkeypatch.setenv("CUPSSGB_FUSE", "1")
+    shapes = [(256, 1, 1), (96, 96, 1), (192, 96, 1), (64, 64, 1), (512, 1, 1)]
+    e = make_ensemble(KPZ)
+    spec = []
+    for i, shape in enumerate(shapes):
+        vals = {"nu": 0.8 + 0.1 * i, "lam": 0.5 + 0.2 * i}
+        init = splitmix64_uniform(int(np.prod(shape)), 300 + i, -0.2, 0.2).reshape(shape[::-1])
+        e.addMember(*shape, dt=0.005, seed=40 + i, **vals)
+        spec.append((shape, vals, 40 + i, init))
+    e.prepare()
+    d = e.describe()
+    assert d["fused"] is not None and d["fused"]["form"] == "fused", d
+    for m, (_, _, _, init) in enumerate(spec):
+        e.setReal(m, "h", init)
+    e.advance(19)
+    for m, (shape, vals, seed, init) in enumerate(spec):
+        ref = plain(KPZ, shape, 0.005, vals, seed, {"h": init}, 19)
+        for nm in ("h", "iqxh", "iqyh"):
+            err = rel(e.getReal(m, nm), ref[nm])
+            assert err < 1e-6, (m, shape, nm, err)
+    e.close()

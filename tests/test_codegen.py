@@ -220,3 +220,26 @@ def test_merge_needs_equal_prefactors_and_exclusive_products(built_lib):
     assert "kNProd = 2;" in src1    # phi^3, and vx*iqxphi + vy*iqyphi
     assert "kNProd = 2;" in src0    # iqxphi*lapphi, iqyphi*lapphi: each used with several prefactors
     s.close()
+
+
+@pytest.mark.parametrize("b,merged", [(1.0, True), (2.0, False)])
+def test_merge_only_with_identical_prefactors(built_lib, b, merged):
+    """dt phi = a*phi^2 + b*psi^2: one channel when a == b, two otherwise; in a batch, one
+    member with a different b keeps the products apart for all."""
+    from tests.test_parser_parity import build_lib
+    ir = build_lib([("phi", 1), ("psi", 1)], {"a": 1.0, "b": b},
+                   ["dt phi + q^2*phi = a*phi^2 + b*psi^2", "dt psi + q^2*psi = 0"], [])
+    s = solver_from_ir(ir, (32, 32, 1))
+    src = s.generated_sources()[0]
+    assert ("kNProd = 1;" in src) == merged
+    s.close()
+    if merged:
+        from cupss_gb300.capi import Pres
+        s = solver_from_ir(ir, (32, 32, 1))
+        s.set_members(3)
+        fi = [f["name"] for f in ir].index("phi")
+        t = [i for i, term in enumerate(ir[fi]["terms"]) if term["product"] == ["psi", "psi"]][0]
+        pres = ir[fi]["terms"][t]["pres"]
+        s.set_member_term_pres(2, fi, t, [Pres(p[0] * 3.0, *p[1:]) for p in pres])
+        assert "kNProd = 2;" in s.generated_sources()[0]
+        s.close()

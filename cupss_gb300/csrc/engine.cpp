@@ -334,17 +334,21 @@ void Solver::check_merges() {
   if (!merge_check_) return;
   merge_check_ = false;
   if (merge_off_ || merges_hold()) return;
-  // re-plan without merging; every distinct product keeps the buffer it has
+  // re-plan without merging: a product keeps the buffer it has (a merged channel's is its
+  // last product's); the others get one now
   merge_off_ = true;
+  const size_t hall = half_ * (size_t)nmem_;
   for (Phase& P : phases_) {
     std::vector<std::pair<std::vector<int>, float2*>> bufs;
-    for (size_t q = 0; q < P.products.size() && q < P.prodbuf.size(); ++q) bufs.push_back({P.products[q], P.prodbuf[q]});
+    for (size_t q = 0; q < P.products.size() && q < P.prodbuf.size(); ++q)
+      if (P.prodbuf[q]) bufs.push_back({P.products[q], P.prodbuf[q]});
     plan_products(P, false);
-    P.prodbuf.clear();
-    for (const auto& key : P.products)
+    P.prodbuf.assign(P.products.size(), nullptr);
+    for (size_t q = 0; q < P.products.size(); ++q) {
       for (const auto& b : bufs)
-        if (b.first == key) P.prodbuf.push_back(b.second);
-    if (P.prodbuf.size() != P.products.size()) throw Error(kErrState, "product buffers lost in re-planning");
+        if (b.first == P.products[q]) P.prodbuf[q] = b.second;
+      if (!P.prodbuf[q]) P.prodbuf[q] = (float2*)dalloc(hall * sizeof(float2));
+    }
     P.jit_sig.clear();
   }
   ++plan_epoch_;
@@ -407,9 +411,11 @@ void Solver::prepare() {
       if (dim_ == 3) chanz_[f] = (float2*)dalloc(hall * sizeof(float2));
     }
   }
-  for (Phase& P : phases_)
-    for (size_t j = 0; j < P.products.size(); ++j)
-      P.prodbuf.push_back((float2*)dalloc(hall * sizeof(float2)));
+  // one buffer per product channel (a merged channel's sits at its last product)
+  for (Phase& P : phases_) {
+    P.prodbuf.assign(P.products.size(), nullptr);
+    for (int c = 0; c < P.nchan; ++c) P.prodbuf[P.chan_buf[c]] = (float2*)dalloc(hall * sizeof(float2));
+  }
   scratch_real_ = (float*)dalloc(npoints() * sizeof(float));
   scratch_spec_ = (float2*)dalloc(half * sizeof(float2));
   // key, step count and active flag of each member (one for a single system)

@@ -183,7 +183,8 @@ void Solver::zero_dynamic_buffers() {
     if (chanz_[f]) check(cudaMemsetAsync(chanz_[f], 0, bytes, stream_), "buffer reset");
   }
   for (Phase& P : phases_)
-    for (float2* b : P.prodbuf) check(cudaMemsetAsync(b, 0, bytes, stream_), "buffer reset");
+    for (float2* b : P.prodbuf)
+      if (b) check(cudaMemsetAsync(b, 0, bytes, stream_), "buffer reset");
   std::fill(par_.begin(), par_.end(), 0);
 }
 
@@ -473,7 +474,7 @@ size_t Solver::estimate_bytes(int members) {
     b += 2 * arr;
     if (alias_order_[f] > 1) b += (dim_ == 3 ? 2 : 1) * arr;
   }
-  for (const Phase& P : phases_) b += P.products.size() * arr;
+  for (const Phase& P : phases_) b += (size_t)P.nchan * arr;   // one buffer per product channel
   if (members > 1 || batch_) b += (size_t)members * (sizeof(MemberK) + 2 * kMemberVals * sizeof(float));
   return b;
 }

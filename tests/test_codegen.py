@@ -243,3 +243,24 @@ def test_merge_only_with_identical_prefactors(built_lib, b, merged):
         s.set_member_term_pres(2, fi, t, [Pres(p[0] * 3.0, *p[1:]) for p in pres])
         assert "kNProd = 2;" in s.generated_sources()[0]
         s.close()
+
+
+def test_merge_groups_only_exclusive_products(built_lib):
+    """phi: a*phi^2 + a*psi^2 + c*phi*psi; psi: a*psi^2.  psi^2 is used by both fields, so
+    only phi^2 could merge -- and alone it stays its own channel: three channels.  With
+    psi's term removed, phi^2 and psi^2 (equal prefactors) share one: two channels."""
+    from tests.test_parser_parity import build_lib
+    params = {"a": 1.0, "c": 2.0}
+    shared = build_lib([("phi", 1), ("psi", 1)], params,
+                       ["dt phi + q^2*phi = a*phi^2 + a*psi^2 + c*phi*psi", "dt psi + q^2*psi = a*psi^2"], [])
+    s = solver_from_ir(shared, (32, 32, 1))
+    assert "kNProd = 3;" in s.generated_sources()[0]
+    s.close()
+    alone = build_lib([("phi", 1), ("psi", 1)], params,
+                      ["dt phi + q^2*phi = a*phi^2 + a*psi^2 + c*phi*psi", "dt psi + q^2*psi = 0"], [])
+    s = solver_from_ir(alone, (32, 32, 1))
+    src = s.generated_sources()[0]
+    assert "kNProd = 2;" in src
+    from cupss_gb300.api import jit_check
+    assert jit_check(src) > 0
+    s.close()

@@ -494,13 +494,16 @@ def bench_served(args):
         for nm, arr in initial_fields(r).items():
             e.setReal(nm, arr)
         e.prepareProblem()
+        t_adv = time.perf_counter()
         e.advanceTime(steps or r["steps"])
         out = e.getReal(sd["out"])
+        t_adv = time.perf_counter() - t_adv
         e.close()
-        return out
+        return out, t_adv
 
     for sysname, shape, dt in keys:   # compile the plain path's programs
         plain_solve(dict(system=sysname, shape=shape, dt=dt, params={}, seed=0, init_seed=0), steps=1)
+
 
     clocks = Clocks(0)
     clocks.start()
@@ -524,12 +527,13 @@ def bench_served(args):
     srv.close()
 
     # plain: service time of each request alone, FIFO in arrival order
-    svc = []
+    svc, adv = [], []
     agree = 0
     for r, got in zip(reqs, served):
         t1 = time.perf_counter()
-        ref = plain_solve(r)
+        ref, t_adv = plain_solve(r)
         svc.append(time.perf_counter() - t1)
+        adv.append(t_adv)
         fa, fb = bool(np.isfinite(ref).all()), bool(np.isfinite(got).all())
         if fa and fb:
             d = np.linalg.norm(got.astype(np.float64) - ref) / max(np.linalg.norm(ref), 1e-30)
@@ -560,6 +564,19 @@ def bench_served(args):
                                  "what": "each request alone: evolver create + prepare + advance + getReal, "
                                          "FIFO in arrival order (programs precompiled)"},
             "speedup_vs_plain": (done - reqs[0]["arrival"]) / makespan,
+            # no schedule ends before a request's arrival plus its steps run alone (advance +
+            # read-back with the GPU to itself): the ratio any server could reach on this stream
+            "bound": {"latest_alone_end_s": max(r["arrival"] + a for r, a in zip(reqs, adv)),
+                      "ratio_upper_bound": (done - reqs[0]["arrival"]) /
+                                           max(r["arrival"] + a for r, a in zip(reqs, adv)),
+                      "alone_s_total": float(sum(adv)),
+                      # requests of >= 2^20 grid points keep the whole GPU busy alone: their
+                      # alone times add up even when they share it
+                      "large_alone_s_total": float(sum(a for r, a in zip(reqs, adv)
+                                                       if np.prod(r["shape"]) >= (1 << 20))),
+                      "what": "latest (arrival + alone advance time) over the requests; ratio_upper_bound = "
+                              "plain FIFO time / that; large_alone_s_total: the alone advance time of the "
+                              "requests of >= 2^20 grid points"},
             "accuracy": {"requests_equal_to_plain": int(agree), "tolerance": "rel L2 1e-6"},
             "server_stats": stats, "warm_s": warm_s, "clocks": clk}
     # the requests that finished last: (system, grid, steps, admitted after, latency) in s

@@ -264,3 +264,42 @@ def test_merge_groups_only_exclusive_products(built_lib):
     from cupss_gb300.api import jit_check
     assert jit_check(src) > 0
     s.close()
+
+
+def test_fused_block_ranges_cover_every_tile(built_lib):
+    """The fused turnaround's blockIdx.x ranges: contiguous, one per grid class, each as
+    long as ceil((sx/2) / W_c) for the class's tile width W_c, and W_c * M_c the same
+    thread count for every class (M_c threads per line); the row pass's ranges hold
+    ceil(sy / RW_c) blocks of 128 threads (M_c * RW_c = 128)."""
+    import re
+    from cupss_gb300.api import multi_generated_sources
+    from tests.test_parser_parity import build_lib
+    shapes = [(512, 512, 1), (256, 256, 1), (96, 96, 1), (256, 1, 1), (64, 128, 1)]
+    solvers = [batched(build_lib(*KPZ_IR), sh) for sh in shapes]
+    _, src = multi_generated_sources(solvers)
+    turn = src[src.index("cupssgb_turn_multi"):src.index("cupssgb_row_multi")]
+    row = src[src.index("cupssgb_row_multi"):]
+    threads = int(re.search(r"__launch_bounds__\((\d+), \d+\) cupssgb_turn_multi", src).group(1))
+    ends = [int(x) for x in re.findall(r"if \(bx < (\d+)\)", turn)]
+    calls = re.findall(r"turn_body_at<(\d+), 1, [^>]*>\(MP\.p\[(\d)\], bx - (\d+), 0, tid % (\d+), tid / (\d+), 0\)",
+                       turn)
+    assert len(ends) == len(calls) == len(shapes)
+    start = 0
+    for c, ((L, idx, b0, W, W2), end, (sx, sy, sz)) in enumerate(zip(calls, ends, shapes)):
+        assert int(idx) == c and int(b0) == start and W == W2 and int(L) == sy
+        W = int(W)
+        assert threads % W == 0
+        assert end - start == -(-(sx // 2) // W), (c, end - start, sx, W)
+        start = end
+    rends = [int(x) for x in re.findall(r"if \(bx < (\d+)\)", row)]
+    rcalls = re.findall(r"(row_one_body|row_pass_body)<(\d+), (true|false)>\(MP\.x\[(\d)\], bx - (\d+), tid % (\d+), "
+                        r"tid / (\d+)\)", row)
+    assert len(rends) == len(rcalls) == len(shapes)
+    start = 0
+    for c, ((_, LX, _, idx, b0, M, M2), end, (sx, sy, sz)) in enumerate(zip(rcalls, rends, shapes)):
+        assert int(idx) == c and int(b0) == start and M == M2 and int(LX) == sx // 2
+        rw = 128 // int(M)
+        assert end - start == -(-(sy * sz) // rw), (c, end - start, sy, rw)
+        start = end
+    for s in solvers:
+        s.close()
